@@ -1,0 +1,385 @@
+"""Benchmark of the cubff epoch step (mutate -> pair -> run -> split) on one GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Workload: bff_noheads, 2^17 programs x 64-byte tapes, uniform random init from
+seed 1, mutation 2^-12 (2^18 / 2^30), Fisher-Yates permutation pairing,
+8192-step limit.  One step = one epoch.  The timed region runs epochs
+0 .. K-1 of a fresh soup (the warm-up runs W epochs of a separate soup), so
+both arms time the same epoch range of the same seeded workload.
+
+Metric: interpreter steps/s as the reference counts them (non-no-op steps,
+common_language.h:192 / bff.inc.h:388), bit-exact.  Also reported: raw
+interpreter iterations/s (the roofline unit), pairs/s, the batched-vs-per-soup
+comparison, the CPU baseline and the integer-issue roofline.
+
+ours:      `value` = device time of the epoch kernels (+ amortised pairing
+           kernels) measured per epoch with CUDA events on the launching
+           stream, L2 flushed between epochs outside the events; `e2e` = the
+           same K epochs through the C ABI (cubff_soup_write / _run / _read)
+           with host buffers, wall clock.
+reference: the reference's CPU implementation on this host's cores (its own
+           build where it compiled on this machine, else the oracle port),
+           bounded to ~60 s of work.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+if REPO not in sys.path:
+    sys.path.insert(0, REPO)
+
+LANG = "bff_noheads"
+N = 1 << 17
+SEED = 1
+MUT = 1 << 18
+K_LANG = {"bff_noheads": 8, "bff": 8, "forth": 10, "subleq": 12, "rsubleq4": 14}
+METRIC = "interp steps/s (reference-counted), bit-exact"
+CONFIG = {"workload": "bff_noheads 2^17 programs x 64 B, seed 1, mutation 2^-12, "
+                      "permutation pairing, 8192-step limit; one step = one epoch",
+          "language": LANG, "num_programs": N, "seed": SEED, "mutation_prob_q30": MUT,
+          "l2": "flushed (256 MiB write) between timed epochs, outside the events"}
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=2048)
+    ap.add_argument("--warmup", type=int, default=8)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-batch", action="store_true")
+    return ap.parse_args()
+
+
+def dist_info():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def measured_peaks():
+    p = os.path.join(REPO, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            return json.load(f), "measured"
+    return {"sm_max_mhz": 2070.0, "hbm_gbs": 6800.0}, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int = 0):
+        self.index = index
+        self.rows = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) >= 9:
+                self.rows.append(parts)
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in self.rows for i in range(4)
+                          if r[5 + i].lower().startswith("active")})
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
+                "samples": len(self.rows)}
+
+
+# ---------------------------------------------------------------------------
+# Our arm.
+
+def gpu_value(torch, abi, steps: int, warmup: int, sm_mhz_hint: float):
+    """Device-timed epochs through the kernel-level C ABI on a torch stream."""
+    from cubff_gb300.workloads import seed_of
+    L = abi.lib()
+    lang = abi.language_id(LANG)
+    dev = torch.device("cuda", 0)
+    stream = torch.cuda.Stream(dev)
+    sp = stream.cuda_stream
+    B = 64  # epochs of pairing per shuffle launch
+    scratch = torch.empty(L.cubff_shuffle_scratch_bytes(N, B), dtype=torch.uint8, device=dev)
+    perm = torch.empty(B * N, dtype=torch.int32, device=dev)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    launches = {"n": 0}
+
+    def run_epochs(first, count, soup, counters, timed):
+        ev = []
+        for i in range(count):
+            e = first + i
+            if timed:
+                flush.fill_(i & 0xFF)  # evict the previous epoch from L2
+                ev.append([torch.cuda.Event(enable_timing=True) for _ in range(3)])
+                ev[-1][0].record(stream)
+            if e % B == 0 or i == 0:
+                abi.check(L.cubff_shuffle_indices(SEED, e, B, N, perm.data_ptr(),
+                                                  scratch.data_ptr(), scratch.numel(), sp))
+                launches["n"] += 6  # memset + 5 pairing kernels
+                base = e
+            if timed:
+                ev[-1][1].record(stream)
+            abi.check(L.cubff_mutate_and_run(
+                lang, soup.data_ptr(), perm.data_ptr() + (e - base) * N * 4, seed_of(SEED, e),
+                MUT, counters.data_ptr() + 16 * i, counters.data_ptr() + 16 * i + 8, N, N // 2, sp))
+            launches["n"] += 1
+            if timed:
+                ev[-1][2].record(stream)
+        return ev
+
+    with torch.cuda.stream(stream):
+        # warm-up on a separate soup
+        wsoup = torch.empty(N * 64, dtype=torch.uint8, device=dev)
+        abi.check(L.cubff_init_programs(seed_of(SEED, 0), N, wsoup.data_ptr(), 0, N, sp))
+        wcnt = torch.zeros(max(warmup, 1) * 2, dtype=torch.int64, device=dev)
+        run_epochs(0, warmup, wsoup, wcnt, False)
+        stream.synchronize()
+        soup = torch.empty(N * 64, dtype=torch.uint8, device=dev)
+        abi.check(L.cubff_init_programs(seed_of(SEED, 0), N, soup.data_ptr(), 0, N, sp))
+        counters = torch.zeros(steps * 2, dtype=torch.int64, device=dev)
+        stream.synchronize()
+        launches["n"] = 0
+        ev = run_epochs(0, steps, soup, counters, True)
+        stream.synchronize()
+    step_ms = [a.elapsed_time(c) for a, b, c in ev]
+    kern_ms = [b.elapsed_time(c) for a, b, c in ev]
+    cnt = counters.view(steps, 2).cpu().numpy()
+    ops, raw = cnt[:, 0].astype("uint64"), cnt[:, 1].astype("uint64")
+    total_s = sum(step_ms) / 1e3
+    return {"total_s": total_s, "step_ms": step_ms, "kern_ms": kern_ms, "ops": ops, "raw": raw,
+            "soup": soup.cpu().numpy(), "launches": launches["n"]}
+
+
+def gpu_e2e(torch, abi, steps: int):
+    """The same epochs through the soup-level C ABI with host buffers:
+    H2D of the initial soup, cubff_soup_run (per-epoch op counts back to the
+    host), D2H of the final soup, wall clock."""
+    import numpy as np
+    eng = abi.Engine(0)
+    ref = abi.Soup(eng, LANG, N, SEED, MUT)
+    init = torch.from_numpy(ref.read()).pin_memory()
+    ref.close()
+    out = torch.empty(N * 64, dtype=torch.uint8).pin_memory()
+    soup = abi.Soup(eng, LANG, N, SEED, MUT)
+    soup.run(1)  # allocate the pairing buffers outside the timed region
+    soup.set_epoch(0, 1)
+    ops = np.zeros(steps, dtype=np.uint64)
+    raw = np.zeros(steps, dtype=np.uint64)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    abi.check(abi.lib().cubff_soup_write(soup.h, init.data_ptr(), 0, N * 64))
+    abi.check(abi.lib().cubff_soup_run(soup.h, steps, ops.ctypes.data, raw.ctypes.data, None, None))
+    abi.check(abi.lib().cubff_soup_read(soup.h, out.data_ptr(), 0, N * 64))
+    torch.cuda.synchronize()
+    dt = time.perf_counter() - t0
+    soup.close()
+    eng.close()
+    return {"total_s": dt, "ops": ops, "raw": raw, "soup": out.numpy().copy()}
+
+
+def batch_compare(torch, abi, epochs: int):
+    """The 64-soup mix (seeds 100..163): one launch per epoch for all soups
+    (cubff_batch_run) against one soup at a time (cubff_soup_run), same GPU,
+    same epochs; op counts must agree."""
+    import numpy as np
+    from cubff_gb300.workloads import batch_mix
+    specs = batch_mix(epochs)
+    eng = abi.Engine(0)
+
+    def make():
+        return [abi.Soup(eng, s.lang, s.num_programs, s.seed, s.mutation_prob) for s in specs]
+
+    soups = make()
+    for s in soups:  # pairing buffers allocated outside the timed region
+        s.run(1)
+        s.set_epoch(0, 1)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    seq_ops = [s.run(epochs)[0] for s in soups]
+    torch.cuda.synchronize()
+    t_seq = time.perf_counter() - t0
+    seq_sha = [hash(s.read().tobytes()) for s in soups]
+    for s in soups:
+        s.close()
+    soups = make()
+    for s in soups:
+        s.run(1)
+        s.set_epoch(0, 1)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    bops = abi.batch_run(eng, soups, epochs)
+    torch.cuda.synchronize()
+    t_bat = time.perf_counter() - t0
+    bat_sha = [hash(s.read().tobytes()) for s in soups]
+    for s in soups:
+        s.close()
+    eng.close()
+    same = all(np.array_equal(a, b) for a, b in zip(seq_ops, bops)) and seq_sha == bat_sha
+    total_ops = float(sum(int(x.sum()) for x in seq_ops))
+    return {"soups": len(specs), "epochs": epochs,
+            "programs_total": int(sum(s.num_programs for s in specs)),
+            "per_soup_steps_per_s": total_ops / t_seq, "batched_steps_per_s": total_ops / t_bat,
+            "batched_over_per_soup": t_seq / t_bat, "bit_identical": bool(same)}
+
+
+def cpu_sample(budget_s: float = 15.0, max_epochs: int = 10**9):
+    """The reference's CPU implementation (its own build when it was compiled
+    on this machine, else the oracle port) on this host's cores, epochs 0..E of
+    the benchmark workload, stopped after ~budget_s."""
+    kind = "port"
+    ref_dir = os.path.join(REPO, "oracle", "_ref")
+    cores = os.cpu_count() or 1
+    ops_total, epochs_run, t_used = 0, 0, 0.0
+    try:
+        sys.path.insert(0, ref_dir)
+        import cubff as refmod  # the reference module, where it was built here
+        kind = "reference"
+    except ImportError:
+        refmod = None
+    finally:
+        if ref_dir in sys.path:
+            sys.path.remove(ref_dir)
+    if refmod is not None:
+        p = refmod.SimulationParams()
+        p.num_programs, p.seed, p.mutation_prob, p.callback_interval = N, SEED, MUT, 1
+        st = {"t0": time.perf_counter(), "ops": 0, "ep": 0}
+
+        def cb(s):
+            st["ops"], st["ep"] = s.total_ops, s.epoch
+            return (time.perf_counter() - st["t0"] > budget_s) or s.epoch >= max_epochs
+        refmod.GetLanguage(LANG).RunSimulation(p, None, cb)
+        t_used = time.perf_counter() - st["t0"]
+        ops_total, epochs_run = st["ops"], st["ep"]
+    else:
+        from oracle import oracle as O
+        O.build()
+        t0 = time.perf_counter()
+        st = {"ops": 0, "ep": 0}
+
+        def cb(e, s, o, r):
+            st["ops"] += o
+            st["ep"] = e
+            return (time.perf_counter() - t0 > budget_s) or e >= max_epochs
+        O.OracleSim(LANG, N, SEED, MUT).run(cb)
+        t_used = time.perf_counter() - t0
+        ops_total, epochs_run = st["ops"], st["ep"]
+    return {"value": ops_total / t_used, "unit": "steps/s", "cores": cores, "kind": kind,
+            "sample": f"{LANG} 2^17 programs seed 1, epochs 0..{epochs_run - 1} "
+                      f"({t_used:.1f} s, callback per epoch)"}
+
+
+def roofline(gv, peaks, peaks_src, sm_mhz):
+    """Integer-issue roofline of the epoch kernel: achieved = raw interpreter
+    iterations x K_lang integer ops per launch / mean launch time; peak =
+    SMs x 128 lane-int-ops/clk x SM clock."""
+    import numpy as np
+    sms = 152
+    try:
+        import torch
+        sms = torch.cuda.get_device_properties(0).multi_processor_count
+    except Exception:
+        pass
+    clk = float(peaks.get("sm_max_mhz", 2070.0))
+    peak = sms * 128 * clk * 1e6 / 1e12           # T int-op/s
+    kern_s = np.array(gv["kern_ms"]) / 1e3
+    achieved = float((gv["raw"].astype(float) * K_LANG[LANG]).sum() / kern_s.sum() / 1e12)
+    return {"bound": "int_issue", "achieved": achieved, "peak": peak, "unit": "Tintop/s",
+            "frac": achieved / peak, "traffic": None,
+            "peak_source": f"{sms} SMs x 128 x {clk:.0f} MHz ({peaks_src} sm_max_mhz)",
+            "hbm_gbs_secondary": float(264.0 * (N // 2) * len(kern_s) / kern_s.sum() / 1e9),
+            "kernel_mean_us": float(kern_s.mean() * 1e6)}
+
+
+def main():
+    args = parse()
+    rank, world, local = dist_info()
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        budget = 60.0
+        s = cpu_sample(budget_s=budget, max_epochs=args.steps)
+        line = {"impl": "reference", "metric": METRIC, "value": s["value"], "unit": "steps/s",
+                "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u8",
+                "data": "synthetic (seeded reference init)", "config": CONFIG,
+                "cpu_baseline": s,
+                "e2e": {"value": s["value"], "unit": "steps/s", "h2d_bytes_per_step": 0,
+                        "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return
+    import numpy as np
+    import torch
+    from cubff_gb300 import abi
+    torch.cuda.set_device(local)
+    abi.lib()
+    peaks, src = measured_peaks()
+    with ClockSampler(local) as clocks:
+        gv = gpu_value(torch, abi, args.steps, args.warmup, peaks.get("sm_max_mhz", 2070.0))
+    ck = clocks.summary()
+    e2 = gpu_e2e(torch, abi, args.steps)
+    assert np.array_equal(gv["ops"], e2["ops"]) and np.array_equal(gv["soup"], e2["soup"]), \
+        "kernel-level and soup-level paths disagree"
+    ops_total = float(gv["ops"].sum())
+    value = ops_total / gv["total_s"] * world
+    line = {"metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": gv["total_s"] * 1e3 / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "u8",
+            "data": "synthetic (seeded reference init)", "config": CONFIG,
+            "raw_steps_per_s": float(gv["raw"].sum()) / gv["total_s"] * world,
+            "pairs_per_s": (N // 2) * args.steps / gv["total_s"] * world,
+            "gpu_launches": gv["launches"],
+            "roofline": roofline(gv, peaks, src, ck.get("sm_mhz")),
+            "clocks": ck,
+            "e2e": {"value": ops_total / e2["total_s"], "unit": "steps/s",
+                    "h2d_bytes_per_step": N * 64 / args.steps,
+                    "d2h_bytes_per_step": (N * 64 + 16 * args.steps) / args.steps,
+                    "wall_s": e2["total_s"]}}
+    if not args.no_batch:
+        line["batched"] = batch_compare(torch, abi, 64)
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_sample()
+    if rank == 0:
+        print(json.dumps(line))
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,183 @@
+"""ctypes binding of the C ABI in include/cubff_gb300.h (libcubff_gb300.so).
+
+This is the binding a Python caller of the engine's C ABI uses; the tests and
+the benchmark call the engine through it.  Loading fails loudly when the
+library has not been built: there is no fallback implementation.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from typing import Optional
+
+import numpy as np
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG, "libcubff_gb300.so")
+
+CUBFF_OK, CUBFF_EINVAL, CUBFF_ENOMEM, CUBFF_EDEVICE, CUBFF_ETIMEDOUT, CUBFF_ENOTFOUND, \
+    CUBFF_EBUSY = range(7)
+PAIR_SHUFFLE, PAIR_FIXED, PAIR_CYCLIC, PAIR_PATTERN = range(4)
+
+u64, u32, vp, ci, cp, sz = (ctypes.c_uint64, ctypes.c_uint32, ctypes.c_void_p, ctypes.c_int,
+                            ctypes.c_char_p, ctypes.c_size_t)
+
+
+class SoupParams(ctypes.Structure):
+    _fields_ = [("lang", ci), ("num_programs", u64), ("seed", u64), ("mutation_prob", u32),
+                ("pairing", ci), ("reset_interval", u64), ("zero_init", ci)]
+
+
+# name -> (restype, argtypes)
+SIGNATURES = {
+    "cubff_status_string": (cp, [ci]),
+    "cubff_last_error": (cp, []),
+    "cubff_language_count": (ci, []),
+    "cubff_language_name": (cp, [ci]),
+    "cubff_language_id": (ci, [cp]),
+    "cubff_init_programs": (ci, [u64, u64, vp, ci, u64, vp]),
+    "cubff_mutate_and_run": (ci, [ci, vp, vp, u64, u32, vp, vp, u64, u64, vp]),
+    "cubff_check_selfrep": (ci, [ci, vp, u64, u64, u64, vp, vp]),
+    "cubff_shuffle_scratch_bytes": (sz, [u64, u32]),
+    "cubff_shuffle_indices": (ci, [u64, u64, u32, u64, vp, vp, sz, vp]),
+    "cubff_engine_create": (ci, [ci, ctypes.POINTER(vp)]),
+    "cubff_engine_destroy": (ci, [vp]),
+    "cubff_soup_create": (ci, [vp, ctypes.POINTER(SoupParams), ctypes.POINTER(vp)]),
+    "cubff_soup_destroy": (ci, [vp]),
+    "cubff_soup_set_pattern": (ci, [vp, vp, vp]),
+    "cubff_soup_write": (ci, [vp, vp, u64, u64]),
+    "cubff_soup_read": (ci, [vp, vp, u64, u64]),
+    "cubff_soup_set_epoch": (ci, [vp, u64, u64]),
+    "cubff_soup_get_epoch": (ci, [vp, vp, vp]),
+    "cubff_soup_run": (ci, [vp, u64, vp, vp, vp, vp]),
+    "cubff_soup_selfrep": (ci, [vp, u64, vp]),
+    "cubff_batch_run": (ci, [vp, vp, ci, u64, vp]),
+}
+
+_lib = None
+
+
+class CubffError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"cubff status {status}: {msg}")
+        self.status = status
+
+
+def lib() -> ctypes.CDLL:
+    """Load libcubff_gb300.so (raises if it has not been built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError(f"{LIB_PATH} is missing: run cubff_gb300.build.build() first")
+        L = ctypes.CDLL(LIB_PATH)
+        for name, (res, args) in SIGNATURES.items():
+            if hasattr(L, name):
+                fn = getattr(L, name)
+                fn.restype = res
+                fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+def check(status: int):
+    if status != CUBFF_OK:
+        raise CubffError(status, lib().cubff_last_error().decode())
+
+
+def language_id(name: str) -> int:
+    i = lib().cubff_language_id(name.encode())
+    if i < 0:
+        raise KeyError(f"unknown language {name!r}")
+    return i
+
+
+def _p(a: Optional[np.ndarray]):
+    return None if a is None else a.ctypes.data_as(vp)
+
+
+class Engine:
+    def __init__(self, device: int = 0):
+        h = vp()
+        check(lib().cubff_engine_create(device, ctypes.byref(h)))
+        self.h = h
+
+    def close(self):
+        if self.h:
+            lib().cubff_engine_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Soup:
+    """A device-resident soup (cubff_soup_*)."""
+
+    def __init__(self, engine: Engine, lang: str, num_programs: int, seed: int = 0,
+                 mutation_prob: int = 1 << 18, pairing: int = PAIR_SHUFFLE,
+                 reset_interval: int = 0, zero_init: bool = False):
+        self.engine = engine
+        self.num_programs = num_programs
+        self.params = SoupParams(language_id(lang), num_programs, seed, mutation_prob, pairing,
+                                 reset_interval, int(zero_init))
+        h = vp()
+        check(lib().cubff_soup_create(engine.h, ctypes.byref(self.params), ctypes.byref(h)))
+        self.h = h
+
+    def set_pattern(self, offs: np.ndarray, tgts: np.ndarray):
+        offs = np.ascontiguousarray(offs, dtype=np.uint32)
+        tgts = np.ascontiguousarray(tgts, dtype=np.uint32)
+        check(lib().cubff_soup_set_pattern(self.h, _p(offs), _p(tgts)))
+
+    def write(self, data: bytes, offset: int = 0):
+        buf = np.frombuffer(bytes(data), dtype=np.uint8)
+        check(lib().cubff_soup_write(self.h, _p(buf), offset, buf.size))
+
+    def read(self) -> np.ndarray:
+        out = np.empty(self.num_programs * 64, dtype=np.uint8)
+        check(lib().cubff_soup_read(self.h, _p(out), 0, out.size))
+        return out
+
+    def set_epoch(self, epoch: int, reset_index: int = 1):
+        check(lib().cubff_soup_set_epoch(self.h, epoch, reset_index))
+
+    def get_epoch(self):
+        e = np.zeros(2, dtype=np.uint64)
+        check(lib().cubff_soup_get_epoch(self.h, _p(e[0:1]), _p(e[1:2])))
+        return int(e[0]), int(e[1])
+
+    def run(self, n_epochs: int, want_shuffle: bool = False):
+        ops = np.zeros(n_epochs, dtype=np.uint64)
+        raw = np.zeros(n_epochs, dtype=np.uint64)
+        shuf = np.zeros(self.num_programs, dtype=np.uint32) if want_shuffle else None
+        ni = np.zeros(1, dtype=np.uint64)
+        check(lib().cubff_soup_run(self.h, n_epochs, _p(ops), _p(raw), _p(shuf), _p(ni)))
+        if want_shuffle:
+            return ops, raw, shuf, int(ni[0])
+        return ops, raw
+
+    def selfrep(self, epoch: int) -> np.ndarray:
+        out = np.zeros(self.num_programs, dtype=np.uint64)
+        check(lib().cubff_soup_selfrep(self.h, epoch, _p(out)))
+        return out
+
+    def close(self):
+        if self.h:
+            lib().cubff_soup_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def batch_run(engine: Engine, soups, n_epochs: int) -> np.ndarray:
+    arr = (vp * len(soups))(*[s.h for s in soups])
+    ops = np.zeros((len(soups), n_epochs), dtype=np.uint64)
+    check(lib().cubff_batch_run(engine.h, arr, len(soups), n_epochs, _p(ops)))
+    return ops

@@ -1,0 +1,507 @@
+// engine.cu — C ABI of the cubff GB300 engine: errors, language registry,
+// kernel-level entry points, and device-resident soups running the epoch loop
+// of Simulation<L>::RunSimulation (common_language.h:345-596).
+#include <algorithm>
+#include <atomic>
+#include <cstdarg>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "common.cuh"
+#include "engine_impl.h"
+#include "internal.h"
+
+namespace cubff {
+
+namespace {
+thread_local std::string g_last_error;
+}
+
+int set_error(int status, const char *fmt, ...) {
+  char buf[1024];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  g_last_error = buf;
+  return status;
+}
+
+void clear_error() { g_last_error.clear(); }
+
+namespace {
+
+const char *const kLangNames[kNumLangs] = {
+    "bff",          "bff_noheads",  "bff_noheads_4bit", "bff_perm",
+    "bff8",         "bff8_noheads", "bff_selfmove",     "forth",
+    "forthcopy",    "forthtrivial", "forthtrivial_reset", "subleq",
+    "rsubleq4"};
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// Host pattern pairing (common_language.h:435-463): serial Fisher-Yates of
+// 0..n-1, then greedy matching in that order, program i proposing neighbour
+// list_i[seed(seed(epoch) ^ seed(i)) % |list_i|].  Unused programs follow in
+// increasing order.  Returns num_indices.
+uint64_t pattern_pairing_host(uint64_t s0, uint64_t epoch, uint64_t n,
+                              const uint32_t *offs, const uint32_t *tgts,
+                              uint32_t *s, std::vector<uint32_t> &order,
+                              std::vector<uint8_t> &used) {
+  order.resize(n);
+  used.assign(n, 0);
+  for (uint64_t i = 0; i < n; i++) order[i] = static_cast<uint32_t>(i);
+  for (uint64_t i = n; i-- > 0;) {
+    const uint64_t j = splitmix64(seed_from(s0, epoch * n + i)) % (i + 1);
+    std::swap(order[i], order[j]);
+  }
+  const uint64_t ek = seed_from(s0, epoch);
+  uint64_t num = 0;
+  for (uint64_t t = 0; t < n; t++) {
+    const uint32_t i = order[t];
+    const uint64_t len = offs[i + 1] - offs[i];
+    if (len == 0) continue;
+    const uint64_t pick = seed_from(s0, ek ^ seed_from(s0, i)) % len;
+    const uint32_t nb = tgts[offs[i] + pick];
+    if (used[i] || used[nb]) continue;
+    used[i] = used[nb] = 1;
+    s[2 * num] = i;
+    s[2 * num + 1] = nb;
+    num++;
+  }
+  uint64_t idx = 2 * num;
+  for (uint64_t i = 0; i < n; i++)
+    if (!used[i]) s[idx++] = static_cast<uint32_t>(i);
+  return num;
+}
+
+}  // namespace cubff
+
+using namespace cubff;
+
+// ---------------------------------------------------------------------------
+// Soup implementation.
+
+static uint32_t pairing_batch(uint64_t n) {
+  // Epochs of pairing computed per launch batch: ~16M draws, at most 64.
+  const uint64_t b = std::max<uint64_t>(1, (uint64_t(1) << 24) / n);
+  return static_cast<uint32_t>(std::min<uint64_t>(b, 64));
+}
+
+static constexpr uint32_t kCounterChunk = 4096;  // epochs of op counters per D2H
+
+int cubff_soup::ensure_buffers() {
+  CUBFF_CUDA_TRY(cudaSetDevice(eng->device));
+  if (!d_perm) {
+    batch = pairing_batch(p.num_programs);
+    CUBFF_CUDA_TRY(cudaMalloc(&d_perm, size_t(batch) * p.num_programs * sizeof(uint32_t)));
+    CUBFF_CUDA_TRY(cudaMalloc(&d_num_indices, size_t(batch) * sizeof(uint64_t)));
+    if (p.pairing == CUBFF_PAIR_SHUFFLE) {
+      scratch_bytes = shuffle_scratch_bytes(p.num_programs, batch);
+      CUBFF_CUDA_TRY(cudaMalloc(&d_scratch, scratch_bytes));
+    }
+    CUBFF_CUDA_TRY(cudaMalloc(&d_counters, size_t(2) * kCounterChunk * sizeof(unsigned long long)));
+    CUBFF_CUDA_TRY(cudaMallocHost(&h_counters, size_t(2) * kCounterChunk * sizeof(unsigned long long)));
+    perm_first = 0;
+    perm_count = 0;
+  }
+  return CUBFF_OK;
+}
+
+void cubff_soup::release() {
+  cudaSetDevice(eng->device);
+  if (d_soup) cudaFree(d_soup);
+  if (d_perm) cudaFree(d_perm);
+  if (d_num_indices) cudaFree(d_num_indices);
+  if (d_scratch) cudaFree(d_scratch);
+  if (d_counters) cudaFree(d_counters);
+  if (h_counters) cudaFreeHost(h_counters);
+  if (h_pat_perm) cudaFreeHost(h_pat_perm);
+  d_soup = nullptr;
+  d_perm = nullptr;
+  d_num_indices = nullptr;
+  d_scratch = nullptr;
+  d_counters = nullptr;
+  h_counters = nullptr;
+  h_pat_perm = nullptr;
+}
+
+// Computes the pairing of epochs [first, first + count) into d_perm.
+int cubff_soup::fill_pairing(uint64_t first, uint32_t count) {
+  cudaStream_t st = eng->stream;
+  const uint64_t n = p.num_programs;
+  switch (p.pairing) {
+    case CUBFF_PAIR_SHUFFLE:
+      CUBFF_TRY(launch_shuffle(s0, first, count, n, d_perm, d_scratch, st));
+      break;
+    case CUBFF_PAIR_FIXED:
+      CUBFF_TRY(launch_fixed(first, count, n, d_perm, st));
+      break;
+    case CUBFF_PAIR_CYCLIC:
+      CUBFF_TRY(launch_cyclic(first, count, n, d_perm, st));
+      break;
+    case CUBFF_PAIR_PATTERN: {
+      if (pat_offs.empty())
+        return set_error(CUBFF_EINVAL, "pattern pairing without interaction lists");
+      if (!h_pat_perm) {
+        CUBFF_CUDA_TRY(cudaMallocHost(&h_pat_perm, (size_t(batch) * n + batch) * sizeof(uint64_t)));
+      }
+      // The previous batch's upload must have finished before the buffer is
+      // rewritten.
+      CUBFF_CUDA_TRY(cudaStreamSynchronize(st));
+      uint32_t *hp = reinterpret_cast<uint32_t *>(h_pat_perm);
+      uint64_t *hn = h_pat_perm + (size_t(batch) * n + 1) / 2;
+      const unsigned hw = std::max(1u, std::min<unsigned>(std::thread::hardware_concurrency(), count));
+      std::vector<std::thread> pool;
+      for (unsigned w = 0; w < hw; w++) {
+        pool.emplace_back([&, w] {
+          std::vector<uint32_t> order;
+          std::vector<uint8_t> used;
+          for (uint32_t e = w; e < count; e += hw)
+            hn[e] = pattern_pairing_host(s0, first + e, n, pat_offs.data(), pat_tgts.data(),
+                                         hp + size_t(e) * n, order, used);
+        });
+      }
+      for (auto &t : pool) t.join();
+      CUBFF_CUDA_TRY(cudaMemcpyAsync(d_perm, hp, size_t(count) * n * sizeof(uint32_t),
+                                     cudaMemcpyHostToDevice, st));
+      CUBFF_CUDA_TRY(cudaMemcpyAsync(d_num_indices, hn, size_t(count) * sizeof(uint64_t),
+                                     cudaMemcpyHostToDevice, st));
+      break;
+    }
+    default:
+      return set_error(CUBFF_EINVAL, "unknown pairing mode %d", p.pairing);
+  }
+  perm_first = first;
+  perm_count = count;
+  return CUBFF_OK;
+}
+
+int cubff_soup::apply_reset() {
+  const uint64_t n = p.num_programs;
+  CUBFF_TRY(launch_init(seed_from(s0, reset_index), n, d_soup, p.zero_init, (n / 32) * 32,
+                        eng->stream));
+  reset_index++;
+  return CUBFF_OK;
+}
+
+int cubff_soup::run(uint64_t n_epochs, uint64_t *ops_out, uint64_t *raw_out, uint32_t *last_shuffle,
+              uint64_t *last_num_indices) {
+  CUBFF_TRY(ensure_buffers());
+  cudaStream_t st = eng->stream;
+  const uint64_t n = p.num_programs;
+  if (pending_reset) {
+    CUBFF_TRY(apply_reset());
+    pending_reset = false;
+  }
+  uint64_t done = 0;
+  while (done < n_epochs) {
+    const uint32_t chunk = static_cast<uint32_t>(std::min<uint64_t>(kCounterChunk, n_epochs - done));
+    CUBFF_CUDA_TRY(cudaMemsetAsync(d_counters, 0, size_t(2) * chunk * sizeof(unsigned long long), st));
+    for (uint32_t c = 0; c < chunk; c++) {
+      const uint64_t e = epoch + done + c;
+      if (perm_count == 0 || e < perm_first || e >= perm_first + perm_count) {
+        const uint64_t remaining = n_epochs - done - c;
+        CUBFF_TRY(fill_pairing(e, static_cast<uint32_t>(std::min<uint64_t>(batch, remaining))));
+      }
+      const uint64_t slot = e - perm_first;
+      EpochArgs a;
+      a.soup = d_soup;
+      a.perm = d_perm + slot * n;
+      a.n = n;
+      a.num_indices = n / 2;
+      a.d_num_indices = p.pairing == CUBFF_PAIR_PATTERN ? d_num_indices + slot : nullptr;
+      a.epoch_key = seed_from(s0, e);
+      a.mutation_prob = p.mutation_prob;
+      a.ops = d_counters + 2 * c;
+      a.raw = d_counters + 2 * c + 1;
+      CUBFF_TRY(launch_epoch(p.lang, a, st));
+      if (p.reset_interval && e % p.reset_interval == 0) {
+        if (done + c + 1 == n_epochs) pending_reset = true;
+        else CUBFF_TRY(apply_reset());
+      }
+    }
+    CUBFF_CUDA_TRY(cudaMemcpyAsync(h_counters, d_counters,
+                                   size_t(2) * chunk * sizeof(unsigned long long),
+                                   cudaMemcpyDeviceToHost, st));
+    CUBFF_CUDA_TRY(cudaStreamSynchronize(st));
+    for (uint32_t c = 0; c < chunk; c++) {
+      if (ops_out) ops_out[done + c] = h_counters[2 * c];
+      if (raw_out) raw_out[done + c] = h_counters[2 * c + 1];
+    }
+    done += chunk;
+  }
+  const uint64_t last = epoch + n_epochs - 1;
+  epoch += n_epochs;
+  if (n_epochs > 0 && (last_shuffle || last_num_indices)) {
+    const uint64_t slot = last - perm_first;
+    if (last_shuffle)
+      CUBFF_CUDA_TRY(cudaMemcpyAsync(last_shuffle, d_perm + slot * n, n * sizeof(uint32_t),
+                                     cudaMemcpyDeviceToHost, st));
+    if (last_num_indices) {
+      if (p.pairing == CUBFF_PAIR_PATTERN)
+        CUBFF_CUDA_TRY(cudaMemcpyAsync(last_num_indices, d_num_indices + slot, sizeof(uint64_t),
+                                       cudaMemcpyDeviceToHost, st));
+      else
+        *last_num_indices = n / 2;
+    }
+    CUBFF_CUDA_TRY(cudaStreamSynchronize(st));
+  }
+  return CUBFF_OK;
+}
+
+
+extern "C" {
+
+const char *cubff_status_string(int status) {
+  switch (status) {
+    case CUBFF_OK: return "ok";
+    case CUBFF_EINVAL: return "invalid argument";
+    case CUBFF_ENOMEM: return "out of memory";
+    case CUBFF_EDEVICE: return "device error";
+    case CUBFF_ETIMEDOUT: return "timed out";
+    case CUBFF_ENOTFOUND: return "not found";
+    case CUBFF_EBUSY: return "busy";
+  }
+  return "unknown status";
+}
+
+const char *cubff_last_error(void) { return g_last_error.c_str(); }
+
+int cubff_language_count(void) { return kNumLangs; }
+
+const char *cubff_language_name(int lang) {
+  return (lang >= 0 && lang < kNumLangs) ? kLangNames[lang] : nullptr;
+}
+
+int cubff_language_id(const char *name) {
+  if (!name) return -1;
+  for (int i = 0; i < kNumLangs; i++)
+    if (std::strcmp(kLangNames[i], name) == 0) return i;
+  return -1;
+}
+
+int cubff_init_programs(uint64_t key, uint64_t num_programs, uint8_t *d_programs,
+                        int zero_init, uint64_t count, void *stream) {
+  if (!d_programs || count > num_programs)
+    return set_error(CUBFF_EINVAL, "init_programs: bad buffer or count");
+  return launch_init(key, num_programs, d_programs, zero_init, count,
+                     static_cast<cudaStream_t>(stream));
+}
+
+int cubff_mutate_and_run(int lang, uint8_t *d_programs, const uint32_t *d_shuf_idx,
+                         uint64_t epoch_key, uint32_t mutation_prob,
+                         unsigned long long *d_insn_count, unsigned long long *d_raw_count,
+                         uint64_t num_programs, uint64_t num_indices, void *stream) {
+  if (lang < 0 || lang >= kNumLangs) return set_error(CUBFF_ENOTFOUND, "unknown language %d", lang);
+  if (!d_programs || !d_shuf_idx || !d_insn_count || num_programs % 2 != 0)
+    return set_error(CUBFF_EINVAL, "mutate_and_run: bad arguments (num_programs must be even)");
+  if ((reinterpret_cast<uintptr_t>(d_programs) & 15) != 0)
+    return set_error(CUBFF_EINVAL, "mutate_and_run: programs buffer must be 16-byte aligned");
+  EpochArgs a;
+  a.soup = d_programs;
+  a.perm = d_shuf_idx;
+  a.n = num_programs;
+  a.num_indices = num_indices;
+  a.d_num_indices = nullptr;
+  a.epoch_key = epoch_key;
+  a.mutation_prob = mutation_prob;
+  a.ops = d_insn_count;
+  a.raw = d_raw_count;
+  return launch_epoch(lang, a, static_cast<cudaStream_t>(stream));
+}
+
+int cubff_check_selfrep(int lang, const uint8_t *d_programs, uint64_t epoch_key,
+                        uint64_t num_programs, uint64_t count, uint64_t *d_result,
+                        void *stream) {
+  if (lang < 0 || lang >= kNumLangs) return set_error(CUBFF_ENOTFOUND, "unknown language %d", lang);
+  if (!d_programs || !d_result || count > num_programs)
+    return set_error(CUBFF_EINVAL, "check_selfrep: bad arguments");
+  return launch_selfrep(lang, d_programs, epoch_key, num_programs, count, d_result,
+                        static_cast<cudaStream_t>(stream));
+}
+
+size_t cubff_shuffle_scratch_bytes(uint64_t num_programs, uint32_t n_epochs) {
+  return shuffle_scratch_bytes(num_programs, n_epochs);
+}
+
+int cubff_shuffle_indices(uint64_t params_seed, uint64_t first_epoch, uint32_t n_epochs,
+                          uint64_t num_programs, uint32_t *d_out, void *d_scratch,
+                          size_t scratch_bytes, void *stream) {
+  if (!d_out || !d_scratch || num_programs == 0 || num_programs > 0xffffffffull)
+    return set_error(CUBFF_EINVAL, "shuffle_indices: bad arguments");
+  if (scratch_bytes < shuffle_scratch_bytes(num_programs, n_epochs))
+    return set_error(CUBFF_EINVAL, "shuffle_indices: scratch too small (%zu < %zu)",
+                     scratch_bytes, shuffle_scratch_bytes(num_programs, n_epochs));
+  return launch_shuffle(splitmix64(params_seed), first_epoch, n_epochs, num_programs, d_out,
+                        d_scratch, static_cast<cudaStream_t>(stream));
+}
+
+int cubff_engine_create(int device, cubff_engine **out) {
+  if (!out) return set_error(CUBFF_EINVAL, "engine_create: null out");
+  int ndev = 0;
+  CUBFF_CUDA_TRY(cudaGetDeviceCount(&ndev));
+  if (device < 0 || device >= ndev)
+    return set_error(CUBFF_EINVAL, "engine_create: device %d of %d", device, ndev);
+  CUBFF_CUDA_TRY(cudaSetDevice(device));
+  auto *e = new (std::nothrow) cubff_engine();
+  if (!e) return set_error(CUBFF_ENOMEM, "engine_create: host allocation");
+  e->device = device;
+  cudaError_t err = cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking);
+  if (err != cudaSuccess) {
+    delete e;
+    return set_error(CUBFF_EDEVICE, "cudaStreamCreate: %s", cudaGetErrorString(err));
+  }
+  *out = e;
+  return CUBFF_OK;
+}
+
+int cubff_engine_destroy(cubff_engine *engine) {
+  if (!engine) return CUBFF_OK;
+  cudaSetDevice(engine->device);
+  cudaStreamSynchronize(engine->stream);
+  engine->release_batch();
+  cudaStreamDestroy(engine->stream);
+  delete engine;
+  return CUBFF_OK;
+}
+
+int cubff_soup_create(cubff_engine *engine, const cubff_soup_params *params,
+                      cubff_soup **out) {
+  if (!engine || !params || !out) return set_error(CUBFF_EINVAL, "soup_create: null argument");
+  const cubff_soup_params &p = *params;
+  if (p.lang < 0 || p.lang >= kNumLangs)
+    return set_error(CUBFF_ENOTFOUND, "soup_create: unknown language %d", p.lang);
+  if (p.num_programs == 0 || p.num_programs % 2 != 0 || p.num_programs > (1ull << 31))
+    return set_error(CUBFF_EINVAL, "soup_create: num_programs %llu must be even, in (0, 2^31]",
+                     static_cast<unsigned long long>(p.num_programs));
+  if (p.pairing < CUBFF_PAIR_SHUFFLE || p.pairing > CUBFF_PAIR_PATTERN)
+    return set_error(CUBFF_EINVAL, "soup_create: unknown pairing %d", p.pairing);
+  if (p.pairing == CUBFF_PAIR_FIXED && (p.num_programs & (p.num_programs - 1)) != 0)
+    return set_error(CUBFF_EINVAL, "soup_create: fixed shuffle needs a power-of-two num_programs");
+  CUBFF_CUDA_TRY(cudaSetDevice(engine->device));
+  auto *s = new (std::nothrow) cubff_soup();
+  if (!s) return set_error(CUBFF_ENOMEM, "soup_create: host allocation");
+  s->eng = engine;
+  s->p = p;
+  s->s0 = splitmix64(p.seed);
+  cudaError_t err = cudaMalloc(&s->d_soup, p.num_programs * kTape);
+  if (err != cudaSuccess) {
+    delete s;
+    return set_error(CUBFF_ENOMEM, "soup_create: cudaMalloc(%llu): %s",
+                     static_cast<unsigned long long>(p.num_programs * kTape),
+                     cudaGetErrorString(err));
+  }
+  int st = launch_init(seed_from(s->s0, 0), p.num_programs, s->d_soup, p.zero_init,
+                       p.num_programs, engine->stream);
+  if (st != CUBFF_OK) {
+    s->release();
+    delete s;
+    return st;
+  }
+  *out = s;
+  return CUBFF_OK;
+}
+
+int cubff_soup_destroy(cubff_soup *soup) {
+  if (!soup) return CUBFF_OK;
+  cudaStreamSynchronize(soup->eng->stream);
+  soup->release();
+  delete soup;
+  return CUBFF_OK;
+}
+
+int cubff_soup_set_pattern(cubff_soup *soup, const uint32_t *offs, const uint32_t *tgts) {
+  if (!soup || !offs) return set_error(CUBFF_EINVAL, "set_pattern: null argument");
+  const uint64_t n = soup->p.num_programs;
+  if (offs[0] != 0) return set_error(CUBFF_EINVAL, "set_pattern: offs[0] must be 0");
+  for (uint64_t i = 0; i < n; i++)
+    if (offs[i + 1] < offs[i]) return set_error(CUBFF_EINVAL, "set_pattern: offs not monotone");
+  const uint64_t ne = offs[n];
+  if (ne && !tgts) return set_error(CUBFF_EINVAL, "set_pattern: null targets");
+  for (uint64_t i = 0; i < n; i++) {
+    for (uint64_t q = offs[i]; q < offs[i + 1]; q++) {
+      if (tgts[q] >= n) return set_error(CUBFF_EINVAL, "set_pattern: target %u out of range", tgts[q]);
+      if (tgts[q] == i)
+        return set_error(CUBFF_EINVAL,
+                         "set_pattern: program %llu lists itself; self-pairs are not supported",
+                         static_cast<unsigned long long>(i));
+    }
+  }
+  soup->pat_offs.assign(offs, offs + n + 1);
+  soup->pat_tgts.assign(tgts, tgts + ne);
+  soup->perm_count = 0;  // cached pairings are stale
+  return CUBFF_OK;
+}
+
+int cubff_soup_write(cubff_soup *soup, const uint8_t *src, uint64_t offset, uint64_t nbytes) {
+  if (!soup || (!src && nbytes)) return set_error(CUBFF_EINVAL, "soup_write: null argument");
+  if (offset + nbytes > soup->p.num_programs * kTape)
+    return set_error(CUBFF_EINVAL, "soup_write: range past the soup");
+  CUBFF_CUDA_TRY(cudaSetDevice(soup->eng->device));
+  CUBFF_CUDA_TRY(cudaMemcpyAsync(soup->d_soup + offset, src, nbytes, cudaMemcpyHostToDevice,
+                                 soup->eng->stream));
+  CUBFF_CUDA_TRY(cudaStreamSynchronize(soup->eng->stream));
+  return CUBFF_OK;
+}
+
+int cubff_soup_read(cubff_soup *soup, uint8_t *dst, uint64_t offset, uint64_t nbytes) {
+  if (!soup || (!dst && nbytes)) return set_error(CUBFF_EINVAL, "soup_read: null argument");
+  if (offset + nbytes > soup->p.num_programs * kTape)
+    return set_error(CUBFF_EINVAL, "soup_read: range past the soup");
+  CUBFF_CUDA_TRY(cudaSetDevice(soup->eng->device));
+  CUBFF_CUDA_TRY(cudaMemcpyAsync(dst, soup->d_soup + offset, nbytes, cudaMemcpyDeviceToHost,
+                                 soup->eng->stream));
+  CUBFF_CUDA_TRY(cudaStreamSynchronize(soup->eng->stream));
+  return CUBFF_OK;
+}
+
+int cubff_soup_set_epoch(cubff_soup *soup, uint64_t epoch, uint64_t reset_index) {
+  if (!soup) return set_error(CUBFF_EINVAL, "set_epoch: null soup");
+  soup->epoch = epoch;
+  soup->reset_index = reset_index;
+  soup->pending_reset = false;
+  return CUBFF_OK;
+}
+
+int cubff_soup_get_epoch(const cubff_soup *soup, uint64_t *epoch, uint64_t *reset_index) {
+  if (!soup) return set_error(CUBFF_EINVAL, "get_epoch: null soup");
+  if (epoch) *epoch = soup->epoch;
+  if (reset_index) *reset_index = soup->reset_index + (soup->pending_reset ? 1 : 0);
+  return CUBFF_OK;
+}
+
+int cubff_soup_run(cubff_soup *soup, uint64_t n_epochs, uint64_t *ops_per_epoch,
+                   uint64_t *raw_per_epoch, uint32_t *last_shuffle, uint64_t *last_num_indices) {
+  if (!soup) return set_error(CUBFF_EINVAL, "soup_run: null soup");
+  if (soup->p.pairing == CUBFF_PAIR_PATTERN && soup->pat_offs.empty())
+    return set_error(CUBFF_EINVAL, "soup_run: pattern pairing needs cubff_soup_set_pattern");
+  CUBFF_CUDA_TRY(cudaSetDevice(soup->eng->device));
+  return soup->run(n_epochs, ops_per_epoch, raw_per_epoch, last_shuffle, last_num_indices);
+}
+
+int cubff_soup_selfrep(cubff_soup *soup, uint64_t epoch, uint64_t *result) {
+  if (!soup || !result) return set_error(CUBFF_EINVAL, "soup_selfrep: null argument");
+  CUBFF_CUDA_TRY(cudaSetDevice(soup->eng->device));
+  const uint64_t n = soup->p.num_programs;
+  const uint64_t count = (n / 32) * 32;  // grid of common_language.h:565
+  uint64_t *d_res = nullptr;
+  CUBFF_CUDA_TRY(cudaMalloc(&d_res, n * sizeof(uint64_t)));
+  int st = CUBFF_OK;
+  cudaError_t err = cudaMemsetAsync(d_res, 0, n * sizeof(uint64_t), soup->eng->stream);
+  if (err == cudaSuccess)
+    st = launch_selfrep(soup->p.lang, soup->d_soup, seed_from(soup->s0, epoch), n, count, d_res,
+                        soup->eng->stream);
+  if (err == cudaSuccess && st == CUBFF_OK)
+    err = cudaMemcpyAsync(result, d_res, n * sizeof(uint64_t), cudaMemcpyDeviceToHost,
+                          soup->eng->stream);
+  if (err == cudaSuccess) err = cudaStreamSynchronize(soup->eng->stream);
+  cudaFree(d_res);
+  if (err != cudaSuccess) return set_error(CUBFF_EDEVICE, "soup_selfrep: %s", cudaGetErrorString(err));
+  return st;
+}
+
+}  // extern "C"

@@ -1,0 +1,178 @@
+/* cubff_gb300.h — C ABI of the GB300 cubff soup engine (libcubff_gb300.so).
+ *
+ * Plain pointers and sizes, integer status returns, no C++ or torch types.
+ * Errors never exit the process: every entry point returns a CUBFF_* status
+ * and cubff_last_error() gives the message of the calling thread's last
+ * failure.
+ *
+ * Three layers:
+ *   1. Kernel-level entry points on caller-owned device buffers: the device
+ *      work of one epoch of the reference, one call per reference launch
+ *      (InitPrograms, MutateAndRunPrograms, CheckSelfRep) plus the pairing
+ *      the reference computes on the host (do_shuffle & friends).
+ *   2. Device-resident soups: the epoch loop of Simulation<L>::RunSimulation
+ *      (common_language.h:345-596) minus the host callback, which the C++ /
+ *      Python layers above drive.
+ *   3. Batching (many soups, one launch per epoch) and serving (continuous
+ *      admission of soup jobs by device-memory footprint).
+ *
+ * Language ids follow the reference's registered names (see
+ * cubff_language_name); pairing modes follow common_language.h:433-486.
+ */
+#ifndef CUBFF_GB300_H_
+#define CUBFF_GB300_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status ------------------------------------------------------------ */
+enum {
+  CUBFF_OK = 0,
+  CUBFF_EINVAL = 1,     /* bad argument (the reference would CHECK-exit)   */
+  CUBFF_ENOMEM = 2,     /* device or host allocation failed                 */
+  CUBFF_EDEVICE = 3,    /* CUDA error (message in cubff_last_error)         */
+  CUBFF_ETIMEDOUT = 4,  /* a bounded wait gave up                           */
+  CUBFF_ENOTFOUND = 5,  /* unknown language / job id                        */
+  CUBFF_EBUSY = 6       /* resource in use (e.g. server at capacity)        */
+};
+
+const char *cubff_status_string(int status);
+/* Message of the calling thread's last failed call ("" if none). */
+const char *cubff_last_error(void);
+
+/* ---- languages ---------------------------------------------------------- */
+/* Registry of the 13 language plugins.  Replaces the REGISTER(L) static
+ * registry and GetLanguage's lookup (common.h:41-45, common.cc:22-40); an
+ * unknown name returns -1 instead of exiting. */
+int cubff_language_count(void);
+const char *cubff_language_name(int lang);
+int cubff_language_id(const char *name);
+
+/* Pairing modes (common_language.h:433-486). */
+enum {
+  CUBFF_PAIR_SHUFFLE = 0, /* permute_programs: Fisher-Yates, :464-477       */
+  CUBFF_PAIR_FIXED = 1,   /* permute_programs && fixed_shuffle, :468-474    */
+  CUBFF_PAIR_CYCLIC = 2,  /* !permute_programs, :478-486                    */
+  CUBFF_PAIR_PATTERN = 3  /* allowed_interactions, :435-463                 */
+};
+
+/* ---- layer 1: kernel-level entry points -------------------------------- */
+/* All pointers named d_* are device pointers; stream is a cudaStream_t (NULL
+ * = legacy default stream).  Calls are asynchronous on the stream. */
+
+/* InitPrograms<L> (common_language.h:138-155; launched at :371-373 and, for
+ * resets, :590-595): programs [0, count) of d_programs get
+ * SplitMix64(64*num_programs*key + 64*idx + i) & 255, or 0 when zero_init. */
+int cubff_init_programs(uint64_t key, uint64_t num_programs,
+                        uint8_t *d_programs, int zero_init, uint64_t count,
+                        void *stream);
+
+/* MutateAndRunPrograms<L> (common_language.h:157-193, launched at :490-493):
+ * pair k < num_programs/2 = programs (d_shuf_idx[2k], d_shuf_idx[2k+1]);
+ * per-byte mutation keyed (num_programs*epoch_key + k)*128 + i; evaluated
+ * (8192-step limit) when k < num_indices; split back.  The epoch's op count
+ * is added to *d_insn_count and, when d_raw_count is not NULL, the raw
+ * interpreter iterations to *d_raw_count.  epoch_key = seed(epoch). */
+int cubff_mutate_and_run(int lang, uint8_t *d_programs,
+                         const uint32_t *d_shuf_idx, uint64_t epoch_key,
+                         uint32_t mutation_prob,
+                         unsigned long long *d_insn_count,
+                         unsigned long long *d_raw_count,
+                         uint64_t num_programs, uint64_t num_indices,
+                         void *stream);
+
+/* CheckSelfRep<L> (common_language.h:203-277, launched at :565-566):
+ * d_result[i] for programs [0, count). */
+int cubff_check_selfrep(int lang, const uint8_t *d_programs, uint64_t epoch_key,
+                        uint64_t num_programs, uint64_t count,
+                        uint64_t *d_result, void *stream);
+
+/* The Fisher-Yates pairing of do_shuffle (common_language.h:418-424, :476)
+ * for n_epochs consecutive epochs, computed on the device:
+ * d_out[e*num_programs + i] = shuffle_idx of epoch first_epoch + e.
+ * params_seed is SimulationParams::seed.  d_scratch must hold
+ * cubff_shuffle_scratch_bytes(num_programs, n_epochs) bytes. */
+size_t cubff_shuffle_scratch_bytes(uint64_t num_programs, uint32_t n_epochs);
+int cubff_shuffle_indices(uint64_t params_seed, uint64_t first_epoch,
+                          uint32_t n_epochs, uint64_t num_programs,
+                          uint32_t *d_out, void *d_scratch,
+                          size_t scratch_bytes, void *stream);
+
+/* ---- layer 2: device-resident soups ------------------------------------ */
+typedef struct cubff_engine cubff_engine;
+typedef struct cubff_soup cubff_soup;
+
+/* SimulationParams (common.h:58-72) fields that shape the epoch step. */
+typedef struct {
+  int lang;                 /* cubff_language_id(...)                      */
+  uint64_t num_programs;    /* even, > 0                                    */
+  uint64_t seed;            /* params.seed                                  */
+  uint32_t mutation_prob;   /* out of 2^30                                  */
+  int pairing;              /* CUBFF_PAIR_*                                 */
+  uint64_t reset_interval;  /* 0 = never                                    */
+  int zero_init;
+} cubff_soup_params;
+
+/* One engine per device (and per host thread driving it). */
+int cubff_engine_create(int device, cubff_engine **out);
+int cubff_engine_destroy(cubff_engine *engine);
+
+/* Allocates the soup on the device and runs the reference's init
+ * (InitPrograms with seed(0), common_language.h:371-373).  The soup starts at
+ * epoch 0 with reset_index 1. */
+int cubff_soup_create(cubff_engine *engine, const cubff_soup_params *params,
+                      cubff_soup **out);
+int cubff_soup_destroy(cubff_soup *soup);
+
+/* allowed_interactions in CSR form (program i may pair with
+ * tgts[offs[i] .. offs[i+1])), for CUBFF_PAIR_PATTERN.  offs has
+ * num_programs+1 entries.  Self-pairs (i listed for i) are rejected. */
+int cubff_soup_set_pattern(cubff_soup *soup, const uint32_t *offs,
+                           const uint32_t *tgts);
+
+/* Host <-> device soup bytes (num_programs * 64 in total).  write is used
+ * for initial_program (:375-378) and for loading a checkpoint (:398-403). */
+int cubff_soup_write(cubff_soup *soup, const uint8_t *src, uint64_t offset,
+                     uint64_t nbytes);
+int cubff_soup_read(cubff_soup *soup, uint8_t *dst, uint64_t offset,
+                    uint64_t nbytes);
+
+/* Epoch counter and reset index (restored from a checkpoint header,
+ * common_language.h:354-360). */
+int cubff_soup_set_epoch(cubff_soup *soup, uint64_t epoch, uint64_t reset_index);
+int cubff_soup_get_epoch(const cubff_soup *soup, uint64_t *epoch,
+                         uint64_t *reset_index);
+
+/* Runs n_epochs epochs of the RunSimulation loop from the soup's epoch:
+ * pairing, MutateAndRunPrograms and resets.  A reset due after the LAST epoch
+ * of the call is applied at the start of the next call, so that the caller's
+ * callback sees the soup as the reference's callback does (:582 before
+ * :590).  ops_per_epoch / raw_per_epoch: host arrays of n_epochs entries
+ * (raw nullable).  last_shuffle (nullable, num_programs entries) receives the
+ * last epoch's shuffle_idx; last_num_indices (nullable) its pair count. */
+int cubff_soup_run(cubff_soup *soup, uint64_t n_epochs,
+                   uint64_t *ops_per_epoch, uint64_t *raw_per_epoch,
+                   uint32_t *last_shuffle, uint64_t *last_num_indices);
+
+/* Self-replication scores of the soup's programs (CheckSelfRep with
+ * seed(epoch)); result has num_programs entries; programs past
+ * (num_programs/32)*32, which the reference's launch does not cover, get 0. */
+int cubff_soup_selfrep(cubff_soup *soup, uint64_t epoch, uint64_t *result);
+
+/* ---- layer 3: batching ------------------------------------------------- */
+/* Advances every soup by n_epochs epochs; each epoch of all soups is one
+ * kernel launch (persistent, soup-descriptor driven) captured in a CUDA graph.
+ * ops: host array [n_soups][n_epochs].  Every soup must belong to engine and
+ * use CUBFF_PAIR_SHUFFLE, FIXED or CYCLIC. */
+int cubff_batch_run(cubff_engine *engine, cubff_soup **soups, int n_soups,
+                    uint64_t n_epochs, uint64_t *ops);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* CUBFF_GB300_H_ */

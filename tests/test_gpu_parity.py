@@ -1,0 +1,183 @@
+"""GPU parity: the engine's CUDA path against the reference fixtures and the
+CPU oracle, through the C ABI.  Every comparison is bit-exact (soup bytes,
+op counts, shuffle indices, self-replication scores)."""
+import os
+
+import numpy as np
+import pytest
+
+from cubff_gb300 import LANGUAGES, abi
+from oracle import oracle as O
+from tests import harness
+from tests.golden_util import load_json, ref_runs
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _cuda():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    abi.lib()
+
+
+RUNS = ref_runs()["runs"]
+
+
+@pytest.mark.parametrize("spec", RUNS, ids=[r["name"] for r in RUNS])
+def test_fixture_run_bit_exact(spec):
+    epochs, ops, shas = harness.gpu_run(spec)
+    assert epochs == spec["epoch"]
+    assert ops == spec["ops"]
+    assert shas == spec["sha"]
+
+
+def _dev(a: np.ndarray):
+    return torch.from_numpy(np.ascontiguousarray(a)).cuda()
+
+
+def _host(t) -> np.ndarray:
+    torch.cuda.synchronize()
+    return t.cpu().numpy()
+
+
+@pytest.mark.parametrize("n", [2, 4, 6, 10, 100, 1000, 4096, 32768])
+def test_shuffle_indices_match_serial_fisher_yates(n):
+    L = abi.lib()
+    seed, first, E = 12345 + n, 17, 3
+    scratch = torch.empty(L.cubff_shuffle_scratch_bytes(n, E), dtype=torch.uint8, device="cuda")
+    out = torch.empty(E * n, dtype=torch.int32, device="cuda")
+    abi.check(L.cubff_shuffle_indices(seed, first, E, n, out.data_ptr(), scratch.data_ptr(),
+                                      scratch.numel(), None))
+    got = _host(out).view(np.uint32).reshape(E, n)
+    for e in range(E):
+        assert np.array_equal(got[e], O.pairing_shuffle(seed, first + e, n)), e
+
+
+def test_shuffle_rejects_small_scratch():
+    L = abi.lib()
+    out = torch.empty(64, dtype=torch.int32, device="cuda")
+    scratch = torch.empty(16, dtype=torch.uint8, device="cuda")
+    st = L.cubff_shuffle_indices(1, 0, 1, 64, out.data_ptr(), scratch.data_ptr(), 16, None)
+    assert st == abi.CUBFF_EINVAL
+
+
+def _command_bytes(lang: str) -> np.ndarray:
+    """Bytes that are commands of the language (dense programs exercise loops,
+    scans, the stack and the 8192-step limit)."""
+    if lang in ("subleq", "rsubleq4"):
+        return np.arange(256, dtype=np.uint8)
+    if lang.startswith("forth"):
+        return np.array(list(range(0, 14)) + list(range(64, 72)) + list(range(128, 136)) +
+                        list(range(192, 200)), dtype=np.uint8)
+    if lang == "bff_noheads_4bit":
+        return np.array([16 * k + v for k in (0, 3, 9) for v in range(16)], dtype=np.uint8)
+    if lang == "bff_perm":
+        return np.arange(0, 11, dtype=np.uint8)
+    if lang == "bff_selfmove":
+        return np.arange(0, 7, dtype=np.uint8)
+    return np.frombuffer(b"[]+-.,<>{}\x00", dtype=np.uint8)
+
+
+@pytest.mark.parametrize("dense", [False, True], ids=["random", "dense"])
+@pytest.mark.parametrize("lang", LANGUAGES)
+def test_mutate_and_run_kernel_matches_oracle(lang, dense):
+    rng = np.random.default_rng(LANGUAGES.index(lang) * 2 + dense)
+    n = 4096
+    if dense:
+        cmds = _command_bytes(lang)
+        soup = cmds[rng.integers(0, cmds.size, n * 64)].astype(np.uint8)
+    else:
+        soup = rng.integers(0, 256, n * 64, dtype=np.uint8)
+    perm = rng.permutation(n).astype(np.uint32)
+    key = int(rng.integers(0, 2**63))
+    prob = 1 << 24
+    num_indices = n // 2 - 7
+    want = soup.copy()
+    want_ops, want_raw = O.mutate_and_run(lang, want, perm, key, prob, num_indices)
+
+    d_soup, d_perm = _dev(soup), _dev(perm.view(np.int32))
+    cnt = torch.zeros(2, dtype=torch.int64, device="cuda")
+    abi.check(abi.lib().cubff_mutate_and_run(
+        abi.language_id(lang), d_soup.data_ptr(), d_perm.data_ptr(), key, prob,
+        cnt.data_ptr(), cnt.data_ptr() + 8, n, num_indices, None))
+    got = _host(d_soup)
+    c = _host(cnt)
+    assert np.array_equal(got, want)
+    assert int(c[0]) == want_ops
+    assert int(c[1]) == want_raw
+
+
+def test_mutate_and_run_self_pair_second_half_wins():
+    """A pair (a, a) scatters the first half, then the second
+    (common_language.h:188-191)."""
+    n = 64
+    rng = np.random.default_rng(5)
+    soup = rng.integers(0, 256, n * 64, dtype=np.uint8)
+    perm = np.arange(n, dtype=np.uint32)
+    perm[0] = perm[1] = 7
+    want = soup.copy()
+    O.mutate_and_run("bff", want, perm, 99, 1 << 20, n // 2)
+    d_soup, d_perm = _dev(soup), _dev(perm.view(np.int32))
+    cnt = torch.zeros(2, dtype=torch.int64, device="cuda")
+    abi.check(abi.lib().cubff_mutate_and_run(abi.language_id("bff"), d_soup.data_ptr(),
+                                             d_perm.data_ptr(), 99, 1 << 20, cnt.data_ptr(),
+                                             None, n, n // 2, None))
+    assert np.array_equal(_host(d_soup), want)
+
+
+@pytest.mark.parametrize("zero_init", [False, True])
+@pytest.mark.parametrize("n,count", [(1000, 1000), (1000, 992), (2, 2), (4096, 4096)])
+def test_init_programs_matches_oracle(n, count, zero_init):
+    key = 0xDEADBEEF12345 + n
+    soup = torch.full((n * 64,), 0xAB, dtype=torch.uint8, device="cuda")
+    abi.check(abi.lib().cubff_init_programs(key, n, soup.data_ptr(), int(zero_init), count, None))
+    want = np.full(n * 64, 0xAB, dtype=np.uint8)
+    O.init_programs(key, n, zero_init, count, want)
+    assert np.array_equal(_host(soup), want)
+
+
+@pytest.mark.parametrize("lang", ["bff", "bff_noheads", "bff8", "forth", "forthtrivial_reset",
+                                  "subleq", "rsubleq4"])
+def test_selfrep_matches_oracle(lang):
+    n = 256
+    sim = O.OracleSim(lang, n, seed=77, mutation_prob=1 << 18)
+    soups = []
+    sim.run(lambda e, s, o, r: soups.append(s.copy()) or e >= 40, 40)
+    soup = soups[-1]
+    key = O.seed_of(77, 40)
+    want = O.check_selfrep(lang, soup, key, n)
+    d_soup = _dev(soup)
+    res = torch.zeros(n, dtype=torch.int64, device="cuda")
+    abi.check(abi.lib().cubff_check_selfrep(abi.language_id(lang), d_soup.data_ptr(), key, n, n,
+                                            res.data_ptr(), None))
+    assert np.array_equal(_host(res).view(np.uint64), want)
+
+
+@pytest.mark.parametrize("lang", ["bff_noheads", "bff", "forth", "subleq"])
+def test_full_size_soup_matches_oracle(lang):
+    """2^17 programs, 6 epochs: soup and per-epoch ops equal the oracle's."""
+    n = 1 << 17
+    spec = {"lang": lang, "num_programs": n, "seed": 1, "epochs": 6}
+    want_ops, want_sha = [], []
+    O.OracleSim(lang, n, 1).run(
+        lambda e, s, o, r: want_ops.append(o) or want_sha.append(O.soup_sha16(s)) or e >= 6)
+    epochs, ops, shas = harness.gpu_run(spec)
+    assert ops == want_ops and shas == want_sha
+
+
+LONG = os.path.join(os.path.dirname(__file__), "golden", "ref_long.json")
+
+
+@pytest.mark.skipif(not os.path.exists(LONG), reason="long fixtures not generated")
+@pytest.mark.parametrize("name", ["long_bff", "long_bff_noheads"])
+def test_long_run_through_emergence(name):
+    """2^17 programs, seed 1: per-256-epoch op counts and soup hashes of the
+    reference through self-replicator emergence."""
+    spec = load_json("ref_long.json")["runs"][name]
+    epochs, ops, shas = harness.gpu_run(spec)
+    assert epochs == spec["epoch"]
+    assert ops == spec["ops"]
+    assert shas == spec["sha"]
