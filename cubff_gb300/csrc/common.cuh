@@ -61,10 +61,10 @@ __device__ __forceinline__ uint32_t lane_base(uint32_t tid) {
 struct LaneBytes {
   uint8_t *s;     // dynamic shared memory block holding the layout
   uint32_t base;  // lane_base(tid)
-  __device__ __forceinline__ uint32_t get(int p) const {
+  __host__ __device__ __forceinline__ uint32_t get(int p) const {
     return s[base + (static_cast<uint32_t>(p) << 7)];
   }
-  __device__ __forceinline__ void set(int p, uint32_t v) const {
+  __host__ __device__ __forceinline__ void set(int p, uint32_t v) const {
     s[base + (static_cast<uint32_t>(p) << 7)] = static_cast<uint8_t>(v);
   }
 };

@@ -4,7 +4,7 @@
 #pragma once
 
 #include "internal.h"
-#include "languages.cuh"
+#include "interp.cuh"
 
 namespace cubff {
 

@@ -1,0 +1,150 @@
+// forth.cuh — the Forth family interpreters (forth, forthcopy, forthtrivial,
+// forthtrivial_reset).
+//
+// Semantics: Stack (forth.inc.h:236-249), EvaluateOne (forth.inc.h:250-373),
+// Evaluate (forth.inc.h:379-397); forthtrivial_reset's Reset / ResetIf and its
+// Write1 / Copy0 (forthtrivial_reset.cu:58-72, :157-166, :215-223).  The
+// stack (128 bytes) lives in shared memory in the same bank-per-lane layout as
+// the tape.
+//
+// Exact cycle fast-forward (cycle.cuh) at backward jumps: the state is
+// (pos, stack pointer, tape, stack contents); a push that stores the value
+// already in its slot and a write that stores the value already in its byte
+// change nothing, so only value-changing stores count as modifications.
+#pragma once
+
+#include "cycle.cuh"
+#include "languages.cuh"
+
+namespace cubff {
+
+static __host__ __device__ __noinline__ void forth_reset(const LaneBytes t, int pos) {
+  uint64_t seed = 0;
+  for (int i = 0; i < kPair; i++) seed = splitmix64(seed ^ t.get(i));
+  for (int i = 0; i < kTape; i++)
+    t.set(i, static_cast<uint32_t>(splitmix64(seed * kTape * kTape +
+                                              static_cast<uint64_t>(pos * kTape) +
+                                              static_cast<uint64_t>(i))));
+}
+
+template <bool kWithReset>
+__host__ __device__ __forceinline__ uint32_t forth_eval(const LaneBytes t, const LaneBytes stk,
+                                               const uint8_t *__restrict__ optab, uint32_t *raw) {
+  int sp = 0;
+  bool overflow = false;
+  uint32_t mods = 0;
+  auto push = [&](uint32_t v) {
+    v &= 0xFF;
+    if (sp != kPair) {
+      if (stk.get(sp) != v) {
+        stk.set(sp, v);
+        mods++;
+      }
+      sp++;
+    } else {
+      overflow = true;
+    }
+  };
+  auto pop = [&]() -> uint32_t { return sp == 0 ? 0u : stk.get(--sp); };
+  auto write = [&](int a, uint32_t v) {
+    v &= 0xFF;
+    if (t.get(a) != v) {
+      t.set(a, v);
+      mods++;
+    }
+  };
+  // Slots at or above sp hold bytes left by an earlier pair; they are never
+  // read before a push overwrites them, and a push compares against whatever
+  // the slot holds, so equal modification counts still imply equal stacks.
+  int pos = 0;
+  uint32_t i = 0, nops = 0;
+  CycleSnap snap;
+  while (true) {
+    const uint32_t c = t.get(pos);
+    bool back = false;
+    switch (optab[c]) {
+      case kRead0: { const int a = pop() % kTape; push(t.get(a)); break; }
+      case kRead1: { const int a = pop() % kTape; push(t.get(kTape + a)); break; }
+      case kRead: { const int a = pop() % kPair; push(t.get(a)); break; }
+      case kWrite: {
+        const uint32_t v = pop();
+        const int a = pop() % kPair;
+        write(a, v);
+        break;
+      }
+      case kWrite0: {
+        const uint32_t v = pop();
+        const int a = pop() % kTape;
+        write(a, v);
+        break;
+      }
+      case kWrite1: {
+        const uint32_t v = pop();
+        const int a = pop() % kTape;
+        if (kWithReset && t.get(kTape + a) == 0x13) {
+          forth_reset(t, pos);
+          mods++;
+        } else {
+          write(kTape + a, v);
+        }
+        break;
+      }
+      case kDup: { const uint32_t v = pop(); push(v); push(v); break; }
+      case kDrop: pop(); break;
+      case kSwap: {
+        const uint32_t a = pop(), b = pop();
+        push(a);
+        push(b);
+        break;
+      }
+      case kIf0: {
+        const uint32_t v = pop();
+        if (v) pos++;
+        push(v);
+        break;
+      }
+      case kInc: push(pop() + 1); break;
+      case kDec: push(pop() - 1); break;
+      case kAdd: { const uint32_t a = pop(), b = pop(); push(a + b); break; }
+      case kSub: { const uint32_t a = pop(), b = pop(); push(a - b); break; }
+      case kConst: push(c & 63); break;
+      case kCopy0: {
+        const int a = pop() % kTape;
+        if (kWithReset && t.get(kTape + a) == 0x13) {
+          forth_reset(t, pos);
+          mods++;
+        } else {
+          write(kTape + a, t.get(a));
+        }
+        break;
+      }
+      case kCopy1: { const int a = pop() % kTape; write(a, t.get(kTape + a)); break; }
+      case kCopy: {
+        const int to = pop() % kPair;
+        const int from = pop() % kPair;
+        write(to, t.get(from));
+        break;
+      }
+      case kXor: push(pop() ^ 64); break;
+      case kJmp: {
+        const int a = (c & 63) + 1;
+        pos += (c & 64) ? -a : a;
+        pos--;
+        back = (c & 64) != 0;
+        break;
+      }
+      default: nops++;
+    }
+    pos++;
+    i++;
+    if (pos >= kPair || pos < 0 || overflow || i >= kStepLimit) break;
+    if (back) {
+      i += snap.visit(pos, sp, 0, mods, i, &nops, kStepLimit);
+      if (i >= kStepLimit) break;
+    }
+  }
+  *raw = i;
+  return i - nops;
+}
+
+}  // namespace cubff
