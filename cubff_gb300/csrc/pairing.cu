@@ -16,6 +16,8 @@
 // Draws are grouped by value with a counting sort (count, scan, fill); next()
 // and parent() are scans of the (small) groups; V follows parent() chains,
 // which strictly increase and so end.
+#include <mutex>
+
 #include "internal.h"
 #include "common.cuh"
 
@@ -214,3 +216,69 @@ int launch_cyclic(uint64_t first_epoch, uint32_t E, uint64_t n, uint32_t *out,
 }
 
 }  // namespace cubff
+
+// ---------------------------------------------------------------------------
+// Allocation-free Fisher-Yates pairing.
+//
+// For callers that cannot allocate device memory themselves: a host
+// application that owns the device allocator (it reserves the GPU's memory up
+// front and forbids other code to call cudaMalloc), or a code path where the
+// implicit device-wide synchronisation of cudaMalloc / cudaFree is not
+// acceptable.  Such a caller passes only its output buffer; the scratch of the
+// pairing kernels is a fixed array in this library's device memory.
+//
+// Limits and behaviour:
+//  * The scratch holds kNoAllocMaxDraws draws (num_programs * n_epochs), i.e.
+//    6 MiB, reserved on every GPU that loads this library until the process
+//    exits.  Larger requests are rejected with CUBFF_EINVAL.
+//  * The first call on a device resolves the array's device address with
+//    cudaGetSymbolAddress (with that device current) and caches it; make that
+//    first call before any stream capture.
+//  * All calls share the one array.  The counts the kernels accumulate are
+//    cleared at the start of every call; everything else is overwritten.
+//    Calls whose work overlaps on the GPU (different streams, or different
+//    host threads without ordering) race on the array: order them.
+namespace cubff {
+namespace {
+
+constexpr uint64_t kNoAllocMaxDraws = uint64_t(1) << 18;
+static __device__ __align__(256) uint32_t g_noalloc_scratch[6 * kNoAllocMaxDraws];
+
+std::mutex g_noalloc_mu;
+void *g_noalloc_addr[64] = {nullptr};
+
+}  // namespace
+
+}  // namespace cubff
+
+extern "C" int cubff_shuffle_indices_noalloc(uint64_t params_seed, uint64_t first_epoch,
+                                             uint32_t n_epochs, uint64_t num_programs,
+                                             uint32_t *d_out, void *stream) {
+  using namespace cubff;
+  if (!d_out || num_programs == 0 || n_epochs == 0)
+    return set_error(CUBFF_EINVAL, "shuffle_indices_noalloc: bad arguments");
+  if (num_programs * n_epochs > kNoAllocMaxDraws)
+    return set_error(CUBFF_EINVAL,
+                     "shuffle_indices_noalloc: num_programs * n_epochs = %llu exceeds the "
+                     "built-in scratch limit of %llu draws",
+                     static_cast<unsigned long long>(num_programs * n_epochs),
+                     static_cast<unsigned long long>(kNoAllocMaxDraws));
+  int dev = 0;
+  CUBFF_CUDA_TRY(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64) return set_error(CUBFF_EINVAL, "shuffle_indices_noalloc: device %d", dev);
+  void *scratch = nullptr;
+  {
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (!g_noalloc_addr[dev]) {
+      void *p = nullptr;
+      cudaError_t err = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+      if (err != cudaSuccess || !p)
+        return set_error(CUBFF_EDEVICE, "shuffle_indices_noalloc: cudaGetSymbolAddress: %s",
+                         cudaGetErrorString(err));
+      g_noalloc_addr[dev] = p;
+    }
+    scratch = g_noalloc_addr[dev];
+  }
+  return launch_shuffle(splitmix64(params_seed), first_epoch, n_epochs, num_programs, d_out,
+                        scratch, static_cast<cudaStream_t>(stream));
+}

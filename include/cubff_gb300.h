@@ -102,6 +102,19 @@ int cubff_shuffle_indices(uint64_t params_seed, uint64_t first_epoch,
                           uint32_t *d_out, void *d_scratch,
                           size_t scratch_bytes, void *stream);
 
+/* Allocation-free variant of cubff_shuffle_indices.  It has no counterpart
+ * in the reference.  It serves callers that cannot allocate device memory
+ * (an application that owns the GPU's allocator, or a path that cannot take
+ * the device-wide synchronisation of cudaMalloc/cudaFree): instead of a
+ * caller-provided scratch buffer it uses a fixed 6 MiB array in this
+ * library's device memory, so num_programs * n_epochs must not exceed 2^18
+ * (larger requests return CUBFF_EINVAL).  The first call on a device looks up
+ * the array's device address (make it before any stream capture).  All calls
+ * share the array, so calls that overlap on the GPU race; order them. */
+int cubff_shuffle_indices_noalloc(uint64_t params_seed, uint64_t first_epoch,
+                                  uint32_t n_epochs, uint64_t num_programs,
+                                  uint32_t *d_out, void *stream);
+
 /* ---- layer 2: device-resident soups ------------------------------------ */
 typedef struct cubff_engine cubff_engine;
 typedef struct cubff_soup cubff_soup;
