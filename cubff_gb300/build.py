@@ -28,7 +28,7 @@ REPO = os.path.dirname(PKG)
 BUILD = os.path.join(PKG, "_build", platform.machine())
 LIB = os.path.join(PKG, "libcubff_gb300.so")
 
-CUDA_SOURCES = ["epoch.cu", "pairing.cu", "engine.cu", "batch.cu"]
+CUDA_SOURCES = ["epoch.cu", "pairing.cu", "pipeline.cu", "engine.cu", "batch.cu"]
 HOST_LIB_SOURCES: list = []
 PY_SOURCES: list = []
 CLI_SOURCES: list = []

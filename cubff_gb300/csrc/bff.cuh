@@ -1,5 +1,5 @@
 // bff.cuh — the BFF family interpreters (bff, bff_noheads, bff_noheads_4bit,
-// bff_perm, bff8, bff8_noheads, bff_selfmove).
+// bff_perm, bff8, bff8_noheads, bff_selfmove) as resumable machines.
 //
 // Semantics: Evaluate (bff.inc.h:356-389), InitialState (bff.inc.h:269-283),
 // EvaluateOne: default (bff.inc.h:289-349), bff8 / bff8_noheads (bff8.cu:23-65),
@@ -7,12 +7,13 @@
 // language's table (optab, BffOp values).
 //
 // Work per step is reduced without changing results:
-//  * three 128-bit masks mark command bytes, '[' bytes and ']' bytes; they are
-//    built once per pair and patched on writes that change a byte's op.
-//  * runs of no-op bytes are crossed in one step of the loop: the reference
-//    counts each as a step and a skip, so i and nskip advance by the run
-//    length (cut at the step limit; a run reaching the tape end ends the run).
-//  * bracket matching walks only the bracket positions of the masks.
+//  * a 128-bit mask marks command bytes; runs of no-op bytes are crossed in
+//    one step of the machine: the reference counts each as a step and a skip,
+//    so i and nskip advance by the run length (cut at the step limit; a run
+//    reaching the tape end ends the program);
+//  * '[' / ']' masks (built on the first loop command) let bracket matching
+//    walk only bracket positions;
+//  * masks are patched on writes that change a byte's op;
 //  * exact cycle fast-forward at backward jumps (cycle.cuh).
 #pragma once
 
@@ -24,30 +25,46 @@ namespace cubff {
 enum BffLogic { kLogicScan, kLogicJump8, kLogicSelfmove };
 
 template <bool kHeads, int kLogic, uint32_t kNullMask>
-__host__ __device__ __forceinline__ uint32_t bff_eval(const LaneBytes t, const uint8_t *__restrict__ optab,
-                                             uint32_t *raw) {
-  Mask128 cmd{0, 0}, opn{0, 0}, cls{0, 0};
-#pragma unroll 8
-  for (int p = 0; p < kPair; p++) {
-    const uint32_t c = optab[t.get(p)];
-    mask_assign(cmd, p, c < kNull);
-    mask_assign(opn, p, c == kLoopStart);
-    mask_assign(cls, p, c == kLoopEnd);
-  }
-  int h0, h1, pc;
-  if (kHeads) {
-    h0 = t.get(0) & (kPair - 1);
-    h1 = t.get(1) & (kPair - 1);
-    pc = 2;
-  } else {
-    h0 = h1 = 0;  // 2 * kSingleTapeSize, masked to 0 at the first step
-    pc = 0;
-  }
-  uint32_t i = 0, nskip = 0, mods = 0;
+struct BffMachine {
+  int pc, h0, h1;
+  uint32_t i, nskip, mods;
+  bool have_brk;
+  Mask128 cmd, opn, cls;
   CycleSnap snap;
 
+  // cmd_mask: bit p set iff tape byte p is a command (op < kNull).
+  __host__ __device__ __forceinline__ void begin(const LaneBytes t, Mask128 cmd_mask) {
+    cmd = cmd_mask;
+    have_brk = false;
+    if (kHeads) {
+      h0 = t.get(0) & (kPair - 1);
+      h1 = t.get(1) & (kPair - 1);
+      pc = 2;
+    } else {
+      h0 = h1 = 0;  // 2 * kSingleTapeSize, masked to 0 at the first step
+      pc = 0;
+    }
+    i = nskip = mods = 0;
+    snap = CycleSnap();
+  }
+
+  __host__ __device__ __forceinline__ void build_brackets(const LaneBytes t,
+                                                          const uint8_t *__restrict__ optab) {
+    opn = Mask128{0, 0};
+    cls = Mask128{0, 0};
+    for (int p = 0; p < kPair; p++) {
+      if (!mask_test(cmd, p)) continue;
+      const uint32_t c = optab[t.get(p)];
+      if (c == kLoopStart) mask_assign(opn, p, true);
+      if (c == kLoopEnd) mask_assign(cls, p, true);
+    }
+    have_brk = true;
+  }
+
   // Writes tape[a] = v (old value o); patches the masks when the op changes.
-  auto write = [&](int a, uint32_t o, uint32_t v) {
+  __host__ __device__ __forceinline__ void write(const LaneBytes t,
+                                                 const uint8_t *__restrict__ optab, int a,
+                                                 uint32_t o, uint32_t v) {
     v &= 0xFF;
     if (v == o) return;
     t.set(a, v);
@@ -55,27 +72,30 @@ __host__ __device__ __forceinline__ uint32_t bff_eval(const LaneBytes t, const u
     const uint32_t co = optab[o], cn = optab[v];
     if (co != cn) {
       mask_assign(cmd, a, cn < kNull);
-      mask_assign(opn, a, cn == kLoopStart);
-      mask_assign(cls, a, cn == kLoopEnd);
+      if (have_brk) {
+        mask_assign(opn, a, cn == kLoopStart);
+        mask_assign(cls, a, cn == kLoopEnd);
+      }
     }
-  };
+  }
 
-  while (true) {
-    // A run of no-op bytes: each is one step and one skip.
+  // One step: a run of no-ops (if any) and then one command.  Returns true
+  // when the program has ended; the op count is then i - nskip.
+  __host__ __device__ __forceinline__ bool step(const LaneBytes t,
+                                                const uint8_t *__restrict__ optab) {
     const int q = mask_next(cmd, pc);
     const uint32_t run = static_cast<uint32_t>(q - pc);
     if (run) {
       if (i + run >= kStepLimit) {
         nskip += kStepLimit - i;
         i = kStepLimit;
-        break;
+        return true;
       }
       i += run;
       nskip += run;
       pc = q;
-      if (pc >= kPair) break;
+      if (pc >= kPair) return true;
     }
-    // One command at pc.
     const uint32_t c = optab[t.get(pc)];
     bool back = false;
     switch (c) {
@@ -83,11 +103,11 @@ __host__ __device__ __forceinline__ uint32_t bff_eval(const LaneBytes t, const u
       case kInc0: h0 = (h0 + 1) & (kPair - 1); break;
       case kDec1: h1 = (h1 - 1) & (kPair - 1); break;
       case kInc1: h1 = (h1 + 1) & (kPair - 1); break;
-      case kPlus: { const uint32_t o = t.get(h0); write(h0, o, o + 1); break; }
-      case kMinus: { const uint32_t o = t.get(h0); write(h0, o, o - 1); break; }
-      case kCopy01: write(h1, t.get(h1), t.get(h0)); break;
+      case kPlus: { const uint32_t o = t.get(h0); write(t, optab, h0, o, o + 1); break; }
+      case kMinus: { const uint32_t o = t.get(h0); write(t, optab, h0, o, o - 1); break; }
+      case kCopy01: write(t, optab, h1, t.get(h1), t.get(h0)); break;
       case kCopy10:
-        write(h0, t.get(h0), t.get(h1));
+        write(t, optab, h0, t.get(h0), t.get(h1));
         if (kLogic == kLogicSelfmove) h1 = (h1 + 1) & (kPair - 1);
         break;
       case kLoopStart:
@@ -95,9 +115,11 @@ __host__ __device__ __forceinline__ uint32_t bff_eval(const LaneBytes t, const u
           if (kLogic == kLogicJump8) {
             pc += 8;
           } else {
+            if (!have_brk) build_brackets(t, optab);
+            const Mask128 brk{opn.lo | cls.lo, opn.hi | cls.hi};
             int depth = 1, p = pc + 1;
             while (true) {
-              const int b = mask_next(Mask128{opn.lo | cls.lo, opn.hi | cls.hi}, p);
+              const int b = mask_next(brk, p);
               if (b >= kPair) { pc = kPair; break; }
               depth += mask_test(opn, b) ? 1 : -1;
               if (depth == 0) { pc = b; break; }
@@ -112,9 +134,11 @@ __host__ __device__ __forceinline__ uint32_t bff_eval(const LaneBytes t, const u
           if (kLogic == kLogicJump8) {
             pc -= 8;
           } else {
+            if (!have_brk) build_brackets(t, optab);
+            const Mask128 brk{opn.lo | cls.lo, opn.hi | cls.hi};
             int depth = 1, p = pc - 1;
             while (true) {
-              const int b = mask_prev(Mask128{opn.lo | cls.lo, opn.hi | cls.hi}, p);
+              const int b = mask_prev(brk, p);
               if (b < 0) { pc = -1; break; }
               depth += mask_test(cls, b) ? 1 : -1;
               if (depth == 0) { pc = b; break; }
@@ -127,16 +151,38 @@ __host__ __device__ __forceinline__ uint32_t bff_eval(const LaneBytes t, const u
         break;
     }
     i++;
-    if (pc < 0) break;
+    if (pc < 0) return true;
     pc++;
-    if (pc >= kPair || i >= kStepLimit) break;
+    if (pc >= kPair || i >= kStepLimit) return true;
     if (back) {
       i += snap.visit(pc, h0, h1, mods, i, &nskip, kStepLimit);
-      if (i >= kStepLimit) break;
+      if (i >= kStepLimit) return true;
     }
+    return false;
   }
-  *raw = i;
-  return i - nskip;
+
+  __host__ __device__ __forceinline__ uint32_t ops() const { return i - nskip; }
+  __host__ __device__ __forceinline__ uint32_t raw() const { return i; }
+};
+
+// Command mask of a staged tape (bit p set iff optab[tape[p]] < kNull).
+__host__ __device__ __forceinline__ Mask128 bff_command_mask(const LaneBytes t,
+                                                             const uint8_t *__restrict__ optab) {
+  Mask128 m{0, 0};
+  for (int p = 0; p < kPair; p++) mask_assign(m, p, optab[t.get(p)] < kNull);
+  return m;
+}
+
+template <bool kHeads, int kLogic, uint32_t kNullMask>
+__host__ __device__ __forceinline__ uint32_t bff_eval(const LaneBytes t,
+                                                      const uint8_t *__restrict__ optab,
+                                                      uint32_t *raw) {
+  BffMachine<kHeads, kLogic, kNullMask> m;
+  m.begin(t, bff_command_mask(t, optab));
+  while (!m.step(t, optab)) {
+  }
+  *raw = m.raw();
+  return m.ops();
 }
 
 }  // namespace cubff

@@ -92,6 +92,9 @@ static uint32_t pairing_batch(uint64_t n) {
 }
 
 static constexpr uint32_t kCounterChunk = 4096;  // epochs of op counters per D2H
+// Counter words: the pipelined runs keep kPipeCountSlots (ops, raw) pairs per
+// epoch; the per-epoch kernels one pair.
+static constexpr size_t kCounterWords = size_t(2) * kPipeCountSlots * kCounterChunk;
 
 int cubff_soup::ensure_buffers() {
   CUBFF_CUDA_TRY(cudaSetDevice(eng->device));
@@ -103,8 +106,13 @@ int cubff_soup::ensure_buffers() {
       scratch_bytes = shuffle_scratch_bytes(p.num_programs, batch);
       CUBFF_CUDA_TRY(cudaMalloc(&d_scratch, scratch_bytes));
     }
-    CUBFF_CUDA_TRY(cudaMalloc(&d_counters, size_t(2) * kCounterChunk * sizeof(unsigned long long)));
-    CUBFF_CUDA_TRY(cudaMallocHost(&h_counters, size_t(2) * kCounterChunk * sizeof(unsigned long long)));
+    CUBFF_CUDA_TRY(cudaMalloc(&d_counters, kCounterWords * sizeof(unsigned long long)));
+    CUBFF_CUDA_TRY(cudaMallocHost(&h_counters, kCounterWords * sizeof(unsigned long long)));
+    CUBFF_CUDA_TRY(cudaMalloc(&d_mutmask, size_t(batch) * (p.num_programs / 2) * sizeof(uint4)));
+    CUBFF_CUDA_TRY(cudaMalloc(&d_ver, p.num_programs * sizeof(uint32_t)));
+    CUBFF_CUDA_TRY(cudaMalloc(&d_ctl, 4 * sizeof(uint32_t)));
+    CUBFF_CUDA_TRY(cudaMemset(d_ctl, 0, 4 * sizeof(uint32_t)));
+    CUBFF_CUDA_TRY(cudaMallocHost(&h_ctl, 4 * sizeof(uint32_t)));
     perm_first = 0;
     perm_count = 0;
   }
@@ -120,6 +128,14 @@ void cubff_soup::release() {
   if (d_counters) cudaFree(d_counters);
   if (h_counters) cudaFreeHost(h_counters);
   if (h_pat_perm) cudaFreeHost(h_pat_perm);
+  if (d_ver) cudaFree(d_ver);
+  if (d_mutmask) cudaFree(d_mutmask);
+  d_mutmask = nullptr;
+  if (d_ctl) cudaFree(d_ctl);
+  if (h_ctl) cudaFreeHost(h_ctl);
+  d_ver = nullptr;
+  d_ctl = nullptr;
+  h_ctl = nullptr;
   d_soup = nullptr;
   d_perm = nullptr;
   d_num_indices = nullptr;
@@ -175,6 +191,7 @@ int cubff_soup::fill_pairing(uint64_t first, uint32_t count) {
     default:
       return set_error(CUBFF_EINVAL, "unknown pairing mode %d", p.pairing);
   }
+  CUBFF_TRY(launch_mutation_masks(s0, first, count, n, p.mutation_prob, d_mutmask, st));
   perm_first = first;
   perm_count = count;
   return CUBFF_OK;
@@ -189,7 +206,7 @@ int cubff_soup::apply_reset() {
 }
 
 int cubff_soup::run(uint64_t n_epochs, uint64_t *ops_out, uint64_t *raw_out, uint32_t *last_shuffle,
-              uint64_t *last_num_indices) {
+                    uint64_t *last_num_indices) {
   CUBFF_TRY(ensure_buffers());
   cudaStream_t st = eng->stream;
   const uint64_t n = p.num_programs;
@@ -200,37 +217,65 @@ int cubff_soup::run(uint64_t n_epochs, uint64_t *ops_out, uint64_t *raw_out, uin
   uint64_t done = 0;
   while (done < n_epochs) {
     const uint32_t chunk = static_cast<uint32_t>(std::min<uint64_t>(kCounterChunk, n_epochs - done));
-    CUBFF_CUDA_TRY(cudaMemsetAsync(d_counters, 0, size_t(2) * chunk * sizeof(unsigned long long), st));
-    for (uint32_t c = 0; c < chunk; c++) {
+    const size_t cwords = size_t(2) * kPipeCountSlots * chunk;
+    CUBFF_CUDA_TRY(cudaMemsetAsync(d_counters, 0, cwords * sizeof(unsigned long long), st));
+    uint32_t c = 0;
+    while (c < chunk) {
       const uint64_t e = epoch + done + c;
       if (perm_count == 0 || e < perm_first || e >= perm_first + perm_count) {
         const uint64_t remaining = n_epochs - done - c;
         CUBFF_TRY(fill_pairing(e, static_cast<uint32_t>(std::min<uint64_t>(batch, remaining))));
       }
+      // One pipelined segment: within the cached pairings and the counter
+      // chunk, ending at the next reset epoch (a reset rewrites every program
+      // at once, common_language.h:590-595).
+      uint64_t seg = std::min<uint64_t>(chunk - c, perm_first + perm_count - e);
+      if (p.reset_interval) {
+        const uint64_t r = e + (p.reset_interval - e % p.reset_interval) % p.reset_interval;
+        seg = std::min<uint64_t>(seg, r - e + 1);
+      }
       const uint64_t slot = e - perm_first;
-      EpochArgs a;
+      CUBFF_CUDA_TRY(cudaMemsetAsync(d_ver, 0, n * sizeof(uint32_t), st));
+      CUBFF_CUDA_TRY(cudaMemsetAsync(d_ctl, 0, 2 * sizeof(uint32_t), st));  // task counter
+      PipeArgs a;
       a.soup = d_soup;
       a.perm = d_perm + slot * n;
       a.n = n;
-      a.num_indices = n / 2;
-      a.d_num_indices = p.pairing == CUBFF_PAIR_PATTERN ? d_num_indices + slot : nullptr;
-      a.epoch_key = seed_from(s0, e);
+      a.s0 = s0;
+      a.e0 = e;
+      a.n_epochs = static_cast<uint32_t>(seg);
       a.mutation_prob = p.mutation_prob;
-      a.ops = d_counters + 2 * c;
-      a.raw = d_counters + 2 * c + 1;
-      CUBFF_TRY(launch_epoch(p.lang, a, st));
-      if (p.reset_interval && e % p.reset_interval == 0) {
-        if (done + c + 1 == n_epochs) pending_reset = true;
+      a.d_num_indices = p.pairing == CUBFF_PAIR_PATTERN ? d_num_indices + slot : nullptr;
+      a.mutmask = d_mutmask + slot * (n / 2);
+      a.ver = d_ver;
+      a.task_counter = reinterpret_cast<unsigned long long *>(d_ctl);
+      a.error = reinterpret_cast<int *>(d_ctl + 2);
+      a.ops = d_counters + size_t(2) * kPipeCountSlots * c;
+      CUBFF_TRY(launch_pipeline(p.lang, a, eng->device, st));
+      const uint64_t last = e + seg - 1;
+      if (p.reset_interval && last % p.reset_interval == 0) {
+        if (done + c + seg == n_epochs) pending_reset = true;
         else CUBFF_TRY(apply_reset());
       }
+      c += static_cast<uint32_t>(seg);
     }
-    CUBFF_CUDA_TRY(cudaMemcpyAsync(h_counters, d_counters,
-                                   size_t(2) * chunk * sizeof(unsigned long long),
+    CUBFF_CUDA_TRY(cudaMemcpyAsync(h_counters, d_counters, cwords * sizeof(unsigned long long),
                                    cudaMemcpyDeviceToHost, st));
+    CUBFF_CUDA_TRY(cudaMemcpyAsync(h_ctl, d_ctl, 4 * sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
     CUBFF_CUDA_TRY(cudaStreamSynchronize(st));
-    for (uint32_t c = 0; c < chunk; c++) {
-      if (ops_out) ops_out[done + c] = h_counters[2 * c];
-      if (raw_out) raw_out[done + c] = h_counters[2 * c + 1];
+    if (h_ctl[2] != 0) {
+      epoch += done;
+      return set_error(CUBFF_ETIMEDOUT,
+                       "soup_run: a pipelined epoch wait timed out; the soup state is invalid");
+    }
+    for (uint32_t q = 0; q < chunk; q++) {
+      uint64_t o = 0, r = 0;
+      for (int sl = 0; sl < kPipeCountSlots; sl++) {
+        o += h_counters[(size_t(q) * kPipeCountSlots + sl) * 2];
+        r += h_counters[(size_t(q) * kPipeCountSlots + sl) * 2 + 1];
+      }
+      if (ops_out) ops_out[done + q] = o;
+      if (raw_out) raw_out[done + q] = r;
     }
     done += chunk;
   }

@@ -39,6 +39,13 @@ struct cubff_soup {
   size_t scratch_bytes = 0;
   uint64_t *h_pat_perm = nullptr;  // pinned staging for host pattern pairings
 
+  // Pipelined runs (pipeline.cu): per-program epoch versions, and the chunk
+  // counter + error flag of the current launch.
+  uint32_t *d_ver = nullptr;
+  uint4 *d_mutmask = nullptr;  // [batch][num_programs / 2] mutation masks
+  uint32_t *d_ctl = nullptr;
+  uint32_t *h_ctl = nullptr;
+
   // Per-epoch op / raw-step counters.
   unsigned long long *d_counters = nullptr;
   unsigned long long *h_counters = nullptr;

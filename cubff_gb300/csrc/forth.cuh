@@ -28,12 +28,24 @@ static __host__ __device__ __noinline__ void forth_reset(const LaneBytes t, int 
 }
 
 template <bool kWithReset>
-__host__ __device__ __forceinline__ uint32_t forth_eval(const LaneBytes t, const LaneBytes stk,
-                                               const uint8_t *__restrict__ optab, uint32_t *raw) {
-  int sp = 0;
-  bool overflow = false;
-  uint32_t mods = 0;
-  auto push = [&](uint32_t v) {
+struct ForthMachine {
+  int pos, sp;
+  bool overflow;
+  uint32_t i, nops, mods;
+  CycleSnap snap;
+
+  // Stack slots at or above sp hold bytes left by an earlier pair; they are
+  // never read before a push overwrites them, and a push compares against
+  // whatever the slot holds, so equal modification counts still imply equal
+  // stacks.
+  __host__ __device__ __forceinline__ void begin() {
+    pos = sp = 0;
+    overflow = false;
+    i = nops = mods = 0;
+    snap = CycleSnap();
+  }
+
+  __host__ __device__ __forceinline__ void push(const LaneBytes stk, uint32_t v) {
     v &= 0xFF;
     if (sp != kPair) {
       if (stk.get(sp) != v) {
@@ -44,88 +56,87 @@ __host__ __device__ __forceinline__ uint32_t forth_eval(const LaneBytes t, const
     } else {
       overflow = true;
     }
-  };
-  auto pop = [&]() -> uint32_t { return sp == 0 ? 0u : stk.get(--sp); };
-  auto write = [&](int a, uint32_t v) {
+  }
+  __host__ __device__ __forceinline__ uint32_t pop(const LaneBytes stk) {
+    return sp == 0 ? 0u : stk.get(--sp);
+  }
+  __host__ __device__ __forceinline__ void write(const LaneBytes t, int a, uint32_t v) {
     v &= 0xFF;
     if (t.get(a) != v) {
       t.set(a, v);
       mods++;
     }
-  };
-  // Slots at or above sp hold bytes left by an earlier pair; they are never
-  // read before a push overwrites them, and a push compares against whatever
-  // the slot holds, so equal modification counts still imply equal stacks.
-  int pos = 0;
-  uint32_t i = 0, nops = 0;
-  CycleSnap snap;
-  while (true) {
+  }
+
+  // One step; returns true when the program has ended (ops = i - nops).
+  __host__ __device__ __forceinline__ bool step(const LaneBytes t, const LaneBytes stk,
+                                                const uint8_t *__restrict__ optab) {
     const uint32_t c = t.get(pos);
     bool back = false;
     switch (optab[c]) {
-      case kRead0: { const int a = pop() % kTape; push(t.get(a)); break; }
-      case kRead1: { const int a = pop() % kTape; push(t.get(kTape + a)); break; }
-      case kRead: { const int a = pop() % kPair; push(t.get(a)); break; }
+      case kRead0: { const int a = pop(stk) % kTape; push(stk, t.get(a)); break; }
+      case kRead1: { const int a = pop(stk) % kTape; push(stk, t.get(kTape + a)); break; }
+      case kRead: { const int a = pop(stk) % kPair; push(stk, t.get(a)); break; }
       case kWrite: {
-        const uint32_t v = pop();
-        const int a = pop() % kPair;
-        write(a, v);
+        const uint32_t v = pop(stk);
+        const int a = pop(stk) % kPair;
+        write(t, a, v);
         break;
       }
       case kWrite0: {
-        const uint32_t v = pop();
-        const int a = pop() % kTape;
-        write(a, v);
+        const uint32_t v = pop(stk);
+        const int a = pop(stk) % kTape;
+        write(t, a, v);
         break;
       }
       case kWrite1: {
-        const uint32_t v = pop();
-        const int a = pop() % kTape;
+        const uint32_t v = pop(stk);
+        const int a = pop(stk) % kTape;
         if (kWithReset && t.get(kTape + a) == 0x13) {
           forth_reset(t, pos);
           mods++;
         } else {
-          write(kTape + a, v);
+          write(t, kTape + a, v);
         }
         break;
       }
-      case kDup: { const uint32_t v = pop(); push(v); push(v); break; }
-      case kDrop: pop(); break;
+      case kDup: { const uint32_t v = pop(stk); push(stk, v); push(stk, v); break; }
+      case kDrop: pop(stk); break;
       case kSwap: {
-        const uint32_t a = pop(), b = pop();
-        push(a);
-        push(b);
+        const uint32_t a = pop(stk), b = pop(stk);
+        push(stk, a);
+        push(stk, b);
         break;
       }
       case kIf0: {
-        const uint32_t v = pop();
+        const uint32_t v = pop(stk);
         if (v) pos++;
-        push(v);
+        push(stk, v);
         break;
       }
-      case kInc: push(pop() + 1); break;
-      case kDec: push(pop() - 1); break;
-      case kAdd: { const uint32_t a = pop(), b = pop(); push(a + b); break; }
-      case kSub: { const uint32_t a = pop(), b = pop(); push(a - b); break; }
-      case kConst: push(c & 63); break;
+      case kInc: push(stk, pop(stk) + 1); break;
+      case kDec: push(stk, pop(stk) - 1); break;
+      case kAdd: { const uint32_t a = pop(stk), b = pop(stk); push(stk, a + b); break; }
+      case kSub: { const uint32_t a = pop(stk), b = pop(stk); push(stk, a - b); break; }
+      case kConst: push(stk, c & 63); break;
       case kCopy0: {
-        const int a = pop() % kTape;
+        const int a = pop(stk) % kTape;
         if (kWithReset && t.get(kTape + a) == 0x13) {
           forth_reset(t, pos);
           mods++;
         } else {
-          write(kTape + a, t.get(a));
+          write(t, kTape + a, t.get(a));
         }
         break;
       }
-      case kCopy1: { const int a = pop() % kTape; write(a, t.get(kTape + a)); break; }
+      case kCopy1: { const int a = pop(stk) % kTape; write(t, a, t.get(kTape + a)); break; }
       case kCopy: {
-        const int to = pop() % kPair;
-        const int from = pop() % kPair;
-        write(to, t.get(from));
+        const int to = pop(stk) % kPair;
+        const int from = pop(stk) % kPair;
+        write(t, to, t.get(from));
         break;
       }
-      case kXor: push(pop() ^ 64); break;
+      case kXor: push(stk, pop(stk) ^ 64); break;
       case kJmp: {
         const int a = (c & 63) + 1;
         pos += (c & 64) ? -a : a;
@@ -137,14 +148,28 @@ __host__ __device__ __forceinline__ uint32_t forth_eval(const LaneBytes t, const
     }
     pos++;
     i++;
-    if (pos >= kPair || pos < 0 || overflow || i >= kStepLimit) break;
+    if (pos >= kPair || pos < 0 || overflow || i >= kStepLimit) return true;
     if (back) {
       i += snap.visit(pos, sp, 0, mods, i, &nops, kStepLimit);
-      if (i >= kStepLimit) break;
+      if (i >= kStepLimit) return true;
     }
+    return false;
   }
-  *raw = i;
-  return i - nops;
+
+  __host__ __device__ __forceinline__ uint32_t ops() const { return i - nops; }
+  __host__ __device__ __forceinline__ uint32_t raw() const { return i; }
+};
+
+template <bool kWithReset>
+__host__ __device__ __forceinline__ uint32_t forth_eval(const LaneBytes t, const LaneBytes stk,
+                                                        const uint8_t *__restrict__ optab,
+                                                        uint32_t *raw) {
+  ForthMachine<kWithReset> m;
+  m.begin();
+  while (!m.step(t, stk, optab)) {
+  }
+  *raw = m.raw();
+  return m.ops();
 }
 
 }  // namespace cubff

@@ -43,7 +43,29 @@ struct EpochArgs {
   unsigned long long *raw;              // += raw iterations (nullable)
 };
 
-// Launchers (epoch.cu / pairing.cu).
+// Launch arguments of a pipelined run of epochs [e0, e0 + n_epochs) of one
+// soup (pipeline.cu).
+struct PipeArgs {
+  uint8_t *soup;
+  const uint32_t *perm;                 // [n_epochs][n] shuffle_idx
+  uint64_t n;
+  uint64_t s0;                          // SplitMix64(params.seed)
+  uint64_t e0;
+  uint32_t n_epochs;
+  uint32_t mutation_prob;
+  const uint64_t *d_num_indices;        // [n_epochs] or nullptr (= n / 2)
+  const uint4 *mutmask;                 // [n_epochs][n / 2] mutation masks
+  uint32_t *ver;                        // [n] epochs completed per program, zeroed
+  unsigned long long *task_counter;     // zeroed
+  int *error;                           // set when a bounded wait gives up
+  unsigned long long *ops;              // [n_epochs][kCountSlots][2]: ops, raw
+};
+constexpr int kPipeCountSlots = 32;
+
+// Launchers (epoch.cu / pairing.cu / pipeline.cu).
+int launch_pipeline(int lang, const PipeArgs &a, int device, cudaStream_t stream);
+int launch_mutation_masks(uint64_t s0, uint64_t e0, uint32_t n_epochs, uint64_t n, uint32_t prob,
+                          uint4 *out, cudaStream_t stream);
 int launch_epoch(int lang, const EpochArgs &a, cudaStream_t stream);
 int launch_init(uint64_t key, uint64_t n, uint8_t *soup, int zero_init,
                 uint64_t count, cudaStream_t stream);

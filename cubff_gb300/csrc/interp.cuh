@@ -4,6 +4,8 @@
 // (Evaluate's return value), reporting the raw loop iterations in *raw.
 #pragma once
 
+#include <type_traits>
+
 #include "bff.cuh"
 #include "forth.cuh"
 #include "languages.cuh"
@@ -36,5 +38,36 @@ __host__ __device__ __forceinline__ uint32_t evaluate(const LaneBytes t, const L
   else if constexpr (L == kSubleq) return subleq_eval(t, raw);
   else return rsubleq4_eval(t, raw);
 }
+
+// A resumable interpreter of language L behind one interface (used by the
+// lane-level pipeline): begin() on a staged tape, step() until it returns
+// true, then ops() / raw().  cmd_mask (BFF family only) marks command bytes.
+template <int L>
+struct LaneMachine {
+  using Machine = std::conditional_t<
+      (L <= kBffSelfmove),
+      BffMachine<(L == kBff || L == kBffPerm || L == kBff8 || L == kBffSelfmove),
+                 (L == kBff8 || L == kBff8Noheads)
+                     ? kLogicJump8
+                     : (L == kBffSelfmove ? kLogicSelfmove : kLogicScan),
+                 (L == kBffNoheads4bit ? 0x0Fu : 0xFFu)>,
+      std::conditional_t<LangTraits<L>::kForthFamily, ForthMachine<(L == kForthtrivialReset)>,
+                         SubleqMachine<(L == kRsubleq4)>>>;
+  Machine m;
+
+  __host__ __device__ __forceinline__ void begin(const LaneBytes t, Mask128 cmd_mask) {
+    if constexpr (L <= kBffSelfmove) m.begin(t, cmd_mask);
+    else m.begin();
+  }
+  __host__ __device__ __forceinline__ bool step(const LaneBytes t, const LaneBytes stk,
+                                                const uint8_t *__restrict__ optab) {
+    if constexpr (L <= kBffSelfmove) return m.step(t, optab);
+    else if constexpr (LangTraits<L>::kForthFamily) return m.step(t, stk, optab);
+    else return m.step(t);
+  }
+  __host__ __device__ __forceinline__ uint32_t ops() const { return m.ops(); }
+  __host__ __device__ __forceinline__ uint32_t raw() const { return m.raw(); }
+  __host__ __device__ __forceinline__ uint32_t mods() const { return m.mods; }
+};
 
 }  // namespace cubff
