@@ -33,6 +33,16 @@ __device__ __forceinline__ uint32_t ld_acquire(const uint32_t *p) {
   return v;
 }
 
+__device__ __forceinline__ uint32_t ld_relaxed(const uint32_t *p) {
+  uint32_t v;
+  asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+__device__ __forceinline__ void fence_acq_rel_gpu() {
+  asm volatile("fence.acq_rel.gpu;" ::: "memory");
+}
+
 __device__ __forceinline__ void st_release(uint32_t *p, uint32_t v) {
   asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
@@ -88,12 +98,21 @@ __global__ void mutation_mask_kernel(uint64_t s0, uint64_t e0, uint64_t npairs, 
 constexpr int kCountSlots = kPipeCountSlots;  // per-epoch counter slots (spread the atomics)
 constexpr int kStepsPerVisit = 4;
 
-// Lane-level dataflow: every lane runs pairs one after another.  Per loop
-// iteration of the warp: idle lanes claim the next pairs (one atomic per
-// warp), waiting lanes test their two programs' versions, ready lanes stage
-// their pair, running lanes advance their interpreter by a few steps, and a
-// finished lane writes its programs back and publishes them.  A pair depends
-// only on the two pairs of the previous epoch that wrote its programs.
+// Lane-level dataflow.  Every lane runs pairs one after another; a pair
+// depends only on the two pairs of the previous epoch that wrote its
+// programs.  Tasks (epoch-major pair order) are dealt out in blocks of 32:
+// warp w owns blocks w, w + W, w + 2W, ... (W = warps in the grid) and its
+// lanes take the block's tasks in order as they become idle.  The lowest
+// unfinished task is always runnable and either held by its owner warp or
+// about to be taken by one of its idle lanes, so the pipeline cannot
+// deadlock.
+//
+// No global access is consumed in the iteration that issues it: the next
+// block's shuffle indices are loaded one block ahead, version polls are
+// relaxed loads read back in the following iteration (with an acquire fence
+// once a pair is ready), and a ready pair's gather lands in registers that
+// are staged into shared memory in the following iteration.  Lane states:
+// idle -> wait -> stage -> run -> (write back, publish) -> idle.
 template <int L>
 __global__ void __launch_bounds__(kThreads) lane_pipeline_kernel(PipeArgs a) {
   extern __shared__ __align__(16) uint8_t smem[];
@@ -113,82 +132,116 @@ __global__ void __launch_bounds__(kThreads) lane_pipeline_kernel(PipeArgs a) {
   const LaneBytes stk{smem + kGroups * kGroupBytes, lane_base(tid)};
   const uint64_t npairs = a.n / 2;
   const uint64_t total = npairs * a.n_epochs;
-  const uint32_t slot = (blockIdx.x * (kThreads / 32) + (tid >> 5)) % kCountSlots;
+  const uint64_t warp_id = uint64_t(blockIdx.x) * (kThreads / 32) + (tid >> 5);
+  const uint64_t n_warps = uint64_t(gridDim.x) * (kThreads / 32);
+  const uint32_t slot = static_cast<uint32_t>(warp_id % kCountSlots);
   const uint32_t lt_mask = (1u << lane) - 1;
 
-  enum : uint32_t { kIdle = 0, kWait = 1, kRun = 2, kDone = 3 };
-  uint32_t state = kIdle, e = 0, p1 = 0, p2 = 0;
+  // Shuffle-index pair (p1 | p2 << 32) of task `task`, or 0 past the end.
+  auto load_qp = [&](uint64_t task) -> uint64_t {
+    if (task >= total) return 0;
+    const uint64_t e = task / npairs, k = task - e * npairs;
+    return *reinterpret_cast<const unsigned long long *>(a.perm + e * a.n + 2 * k);
+  };
+  uint64_t cur_block = warp_id, next_block = warp_id + n_warps;
+  uint64_t cur_qp = load_qp(cur_block * 32 + lane);
+  uint64_t next_qp = load_qp(next_block * 32 + lane);
+  uint32_t used = 0;  // tasks of the current block already taken
+
+  enum : uint32_t { kIdle = 0, kWait = 1, kStage = 2, kRun = 3, kDone = 4 };
+  uint32_t state = kIdle, e = 0, p1 = 0, p2 = 0, v1 = 0, v2 = 0;
   uint64_t k = 0, t_wait = 0;
   bool dirty = false, evaluated = false;
+  uint4 g[8];
+  uint4 mm = make_uint4(0, 0, 0, 0);
   LaneMachine<L> m;
 
   while (true) {
+    // 1. Idle lanes take the next tasks of the warp's blocks.
     const uint32_t idle = __ballot_sync(0xffffffffu, state == kIdle);
     if (idle) {
-      const int leader = __ffs(idle) - 1;
-      unsigned long long base = total;
-      if (lane == static_cast<uint32_t>(leader) && !ld_volatile(a.error))
-        base = atomicAdd(reinterpret_cast<unsigned long long *>(a.task_counter),
-                         static_cast<unsigned long long>(__popc(idle)));
-      base = __shfl_sync(0xffffffffu, base, leader);
+      const uint32_t idx = used + __popc(idle & lt_mask);
+      const uint64_t qa = __shfl_sync(0xffffffffu, cur_qp, idx & 31);
+      const uint64_t qb = __shfl_sync(0xffffffffu, next_qp, idx & 31);
       if (state == kIdle) {
-        const uint64_t task = base + __popc(idle & lt_mask);
-        if (task >= total) {
+        const uint64_t task = idx < 32 ? cur_block * 32 + idx : next_block * 32 + (idx - 32);
+        if (task >= total || ld_volatile(a.error)) {
           state = kDone;
         } else {
           e = static_cast<uint32_t>(task / npairs);
           k = task - uint64_t(e) * npairs;
-          const uint32_t *perm = a.perm + uint64_t(e) * a.n;
-          p1 = perm[2 * k];
-          p2 = perm[2 * k + 1];
+          const uint64_t qp = idx < 32 ? qa : qb;
+          p1 = static_cast<uint32_t>(qp);
+          p2 = static_cast<uint32_t>(qp >> 32);
+          v1 = ld_relaxed(a.ver + p1);
+          v2 = ld_relaxed(a.ver + p2);
           state = kWait;
           t_wait = 0;
         }
+      }
+      used += __popc(idle);
+      if (used >= 32) {  // current block exhausted: advance, prefetch the next
+        used -= 32;
+        cur_block = next_block;
+        cur_qp = next_qp;
+        next_block += n_warps;
+        next_qp = load_qp(next_block * 32 + lane);
       }
     }
     if (__all_sync(0xffffffffu, state == kDone)) break;
     bool progressed = false;
 
-    if (state == kWait) {
-      if (ld_acquire(a.ver + p1) >= e && ld_acquire(a.ver + p2) >= e) {
-        // Stage the pair: gather, mutation (precomputed masks), command mask.
-        uint32_t w[32];
-        load_pair_cg(a.soup, p1, p2, w);
-        Mask128 cmd{0, 0};
+    // 2. Staging: the gather issued in an earlier iteration has landed.
+    if (state == kStage) {
+      Mask128 cmd{0, 0};
 #pragma unroll
-        for (int q = 0; q < 32; q++) {
+      for (int q = 0; q < 32; q++) {
+        const uint32_t w = q % 4 == 0 ? g[q / 4].x : q % 4 == 1 ? g[q / 4].y
+                         : q % 4 == 2 ? g[q / 4].z : g[q / 4].w;
 #pragma unroll
-          for (int b = 0; b < 4; b++) t.set(4 * q + b, w[q] >> (8 * b));
-          if (kBffFam) {
-            const uint32_t f = cmdflag[w[q] & 0xFF] | (cmdflag[(w[q] >> 8) & 0xFF] << 8) |
-                               (cmdflag[(w[q] >> 16) & 0xFF] << 16) |
-                               (cmdflag[w[q] >> 24] << 24);
-            const uint64_t nib = (f * 0x01020408u) >> 24;
-            if (q < 16) cmd.lo |= nib << (4 * q);
-            else cmd.hi |= nib << (4 * (q - 16));
+        for (int b = 0; b < 4; b++) t.set(4 * q + b, w >> (8 * b));
+        if (kBffFam) {
+          const uint32_t f = cmdflag[w & 0xFF] | (cmdflag[(w >> 8) & 0xFF] << 8) |
+                             (cmdflag[(w >> 16) & 0xFF] << 16) | (cmdflag[w >> 24] << 24);
+          const uint64_t nib = (f * 0x01020408u) >> 24;
+          if (q < 16) cmd.lo |= nib << (4 * q);
+          else cmd.hi |= nib << (4 * (q - 16));
+        }
+      }
+      dirty = (mm.x | mm.y | mm.z | mm.w) != 0;
+      if (dirty) {
+        const uint64_t key0 = (a.n * seed_from(a.s0, a.e0 + e) + k) * kPair;
+        const uint32_t mw[4] = {mm.x, mm.y, mm.z, mm.w};
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+          uint32_t bits = mw[q];
+          while (bits) {
+            const int i = q * 32 + __ffs(bits) - 1;
+            bits &= bits - 1;
+            const uint32_t v = static_cast<uint32_t>(splitmix64(key0 + i)) & 0xFFu;
+            t.set(i, v);
+            if (kBffFam) mask_assign(cmd, i, cmdflag[v] != 0);
           }
         }
-        const uint4 mm = a.mutmask[uint64_t(e) * npairs + k];
-        dirty = (mm.x | mm.y | mm.z | mm.w) != 0;
-        if (dirty) {
-          const uint64_t key0 = (a.n * seed_from(a.s0, a.e0 + e) + k) * kPair;
-          const uint32_t mw[4] = {mm.x, mm.y, mm.z, mm.w};
+      }
+      const uint64_t num_indices = a.d_num_indices ? a.d_num_indices[e] : npairs;
+      evaluated = k < num_indices;
+      m.begin(t, cmd);
+      state = kRun;
+      progressed = true;
+    } else if (state == kWait) {
+      // 3. Waiting: versions polled in the previous iteration.
+      if (v1 >= e && v2 >= e) {
+        fence_acq_rel_gpu();  // order the gather after the observed releases
+        const uint4 *g1 = reinterpret_cast<const uint4 *>(a.soup + uint64_t(p1) * kTape);
+        const uint4 *g2 = reinterpret_cast<const uint4 *>(a.soup + uint64_t(p2) * kTape);
 #pragma unroll
-          for (int q = 0; q < 4; q++) {
-            uint32_t bits = mw[q];
-            while (bits) {
-              const int i = q * 32 + __ffs(bits) - 1;
-              bits &= bits - 1;
-              const uint32_t v = static_cast<uint32_t>(splitmix64(key0 + i)) & 0xFFu;
-              t.set(i, v);
-              if (kBffFam) mask_assign(cmd, i, cmdflag[v] != 0);
-            }
-          }
+        for (int q = 0; q < 4; q++) {
+          g[q] = __ldcg(g1 + q);
+          g[4 + q] = __ldcg(g2 + q);
         }
-        const uint64_t num_indices = a.d_num_indices ? a.d_num_indices[e] : npairs;
-        evaluated = k < num_indices;
-        m.begin(t, cmd);
-        state = kRun;
+        mm = __ldg(a.mutmask + uint64_t(e) * npairs + k);
+        state = kStage;
         progressed = true;
       } else if (ld_volatile(a.error)) {
         state = kDone;
@@ -200,10 +253,13 @@ __global__ void __launch_bounds__(kThreads) lane_pipeline_kernel(PipeArgs a) {
           atomicExch(a.error, 1);
           state = kDone;
         }
+        if (state == kWait) {
+          v1 = ld_relaxed(a.ver + p1);
+          v2 = ld_relaxed(a.ver + p2);
+        }
       }
-    }
-
-    if (state == kRun) {
+    } else if (state == kRun) {
+      // 4. Running: a few interpreter steps; finish with write-back + publish.
       progressed = true;
       bool fin = !evaluated;
       for (int r = 0; r < kStepsPerVisit && !fin; r++) fin = m.step(t, stk, optab);
@@ -215,14 +271,14 @@ __global__ void __launch_bounds__(kThreads) lane_pipeline_kernel(PipeArgs a) {
             w[q] = t.get(4 * q) | (t.get(4 * q + 1) << 8) | (t.get(4 * q + 2) << 16) |
                    (t.get(4 * q + 3) << 24);
           // First half, then second half (common_language.h:188-191).
-          uint4 *g1 = reinterpret_cast<uint4 *>(a.soup + uint64_t(p1) * kTape);
-          uint4 *g2 = reinterpret_cast<uint4 *>(a.soup + uint64_t(p2) * kTape);
+          uint4 *o1 = reinterpret_cast<uint4 *>(a.soup + uint64_t(p1) * kTape);
+          uint4 *o2 = reinterpret_cast<uint4 *>(a.soup + uint64_t(p2) * kTape);
 #pragma unroll
           for (int q = 0; q < 4; q++)
-            g1[q] = make_uint4(w[4 * q], w[4 * q + 1], w[4 * q + 2], w[4 * q + 3]);
+            o1[q] = make_uint4(w[4 * q], w[4 * q + 1], w[4 * q + 2], w[4 * q + 3]);
 #pragma unroll
           for (int q = 0; q < 4; q++)
-            g2[q] = make_uint4(w[16 + 4 * q], w[16 + 4 * q + 1], w[16 + 4 * q + 2],
+            o2[q] = make_uint4(w[16 + 4 * q], w[16 + 4 * q + 1], w[16 + 4 * q + 2],
                                w[16 + 4 * q + 3]);
         }
         st_release(a.ver + p1, e + 1);  // orders the tape stores before the flags
@@ -235,7 +291,7 @@ __global__ void __launch_bounds__(kThreads) lane_pipeline_kernel(PipeArgs a) {
         state = kIdle;
       }
     }
-    if (!__any_sync(0xffffffffu, progressed)) __nanosleep(100);
+    if (!__any_sync(0xffffffffu, progressed)) __nanosleep(200);
   }
 }
 
