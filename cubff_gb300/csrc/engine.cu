@@ -4,6 +4,7 @@
 #include <algorithm>
 #include <atomic>
 #include <cstdarg>
+#include <cstdlib>
 #include <cstring>
 #include <mutex>
 #include <string>
@@ -251,6 +252,7 @@ int cubff_soup::run(uint64_t n_epochs, uint64_t *ops_out, uint64_t *raw_out, uin
       a.task_counter = reinterpret_cast<unsigned long long *>(d_ctl);
       a.error = reinterpret_cast<int *>(d_ctl + 2);
       a.ops = d_counters + size_t(2) * kPipeCountSlots * c;
+      a.lanes_per_pair64 = eng->lanes_per_pair64;
       CUBFF_TRY(launch_pipeline(p.lang, a, eng->device, st));
       const uint64_t last = e + seg - 1;
       if (p.reset_interval && last % p.reset_interval == 0) {
@@ -395,6 +397,7 @@ int cubff_engine_create(int device, cubff_engine **out) {
   auto *e = new (std::nothrow) cubff_engine();
   if (!e) return set_error(CUBFF_ENOMEM, "engine_create: host allocation");
   e->device = device;
+  if (const char *v = std::getenv("CUBFF_LANES_PER_PAIR64")) e->lanes_per_pair64 = std::atoi(v);
   cudaError_t err = cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking);
   if (err != cudaSuccess) {
     delete e;

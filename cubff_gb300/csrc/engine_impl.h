@@ -11,6 +11,7 @@
 struct cubff_engine {
   int device = 0;
   cudaStream_t stream = nullptr;
+  uint32_t lanes_per_pair64 = 0;  // pipelined-run lanes in flight per 64 pairs (0 = default)
 
   // Batched-epoch staging (batch.cu): per-epoch soup descriptors and counters.
   void *d_desc = nullptr, *h_desc = nullptr;

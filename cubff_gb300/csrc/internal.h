@@ -59,6 +59,7 @@ struct PipeArgs {
   unsigned long long *task_counter;     // zeroed
   int *error;                           // set when a bounded wait gives up
   unsigned long long *ops;              // [n_epochs][kCountSlots][2]: ops, raw
+  uint32_t lanes_per_pair64;            // lanes in flight per 64 pairs (0 = default)
 };
 constexpr int kPipeCountSlots = 32;
 

@@ -151,6 +151,8 @@ __global__ void __launch_bounds__(kThreads) lane_pipeline_kernel(PipeArgs a) {
   enum : uint32_t { kIdle = 0, kWait = 1, kStage = 2, kRun = 3, kDone = 4 };
   uint32_t state = kIdle, e = 0, p1 = 0, p2 = 0, v1 = 0, v2 = 0;
   uint64_t k = 0, t_wait = 0;
+  uint32_t poll_gap = 1, poll_in = 0;  // per-lane poll backoff (iterations)
+  uint32_t err = 0;                    // error flag as of the last poll
   bool dirty = false, evaluated = false;
   uint4 g[8];
   uint4 mm = make_uint4(0, 0, 0, 0);
@@ -165,7 +167,7 @@ __global__ void __launch_bounds__(kThreads) lane_pipeline_kernel(PipeArgs a) {
       const uint64_t qb = __shfl_sync(0xffffffffu, next_qp, idx & 31);
       if (state == kIdle) {
         const uint64_t task = idx < 32 ? cur_block * 32 + idx : next_block * 32 + (idx - 32);
-        if (task >= total || ld_volatile(a.error)) {
+        if (task >= total) {
           state = kDone;
         } else {
           e = static_cast<uint32_t>(task / npairs);
@@ -177,6 +179,8 @@ __global__ void __launch_bounds__(kThreads) lane_pipeline_kernel(PipeArgs a) {
           v2 = ld_relaxed(a.ver + p2);
           state = kWait;
           t_wait = 0;
+          poll_gap = 1;
+          poll_in = 0;
         }
       }
       used += __popc(idle);
@@ -243,19 +247,26 @@ __global__ void __launch_bounds__(kThreads) lane_pipeline_kernel(PipeArgs a) {
         mm = __ldg(a.mutmask + uint64_t(e) * npairs + k);
         state = kStage;
         progressed = true;
-      } else if (ld_volatile(a.error)) {
-        state = kDone;
-      } else {
-        const uint64_t now = globaltimer_ns();
-        if (t_wait == 0) {
-          t_wait = now;
-        } else if (now - t_wait > kWaitLimitNs) {
-          atomicExch(a.error, 1);
+      } else if (poll_in-- == 0) {
+        // Not ready: the error flag and the deadline are checked on the poll
+        // schedule, and the next poll is issued (read back next time).
+        if (err) {
           state = kDone;
+        } else {
+          const uint64_t now = globaltimer_ns();
+          if (t_wait == 0) {
+            t_wait = now;
+          } else if (now - t_wait > kWaitLimitNs) {
+            atomicExch(a.error, 1);
+            state = kDone;
+          }
         }
         if (state == kWait) {
           v1 = ld_relaxed(a.ver + p1);
           v2 = ld_relaxed(a.ver + p2);
+          err = ld_relaxed(reinterpret_cast<const uint32_t *>(a.error));
+          poll_gap = poll_gap < 16 ? poll_gap * 2 : 16;
+          poll_in = poll_gap;
         }
       }
     } else if (state == kRun) {
@@ -323,8 +334,14 @@ int launch_pipeline_t(const PipeArgs &a, int device, cudaStream_t stream) {
     CUBFF_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
     g = std::max(1, per_sm) * sms;
   }
-  const uint64_t tasks = (a.n / 2) * a.n_epochs;
-  const uint64_t blocks = (tasks + kThreads - 1) / kThreads;
+  // Lanes in flight: enough to keep the SMs busy, few enough that most held
+  // pairs are ready (a lane holding a pair of a later epoch only polls).
+  // lanes_per_pair (x1/64) is tunable; the default keeps half an epoch of
+  // pairs in flight.
+  const uint64_t npairs = a.n / 2;
+  uint64_t want = (npairs * static_cast<uint64_t>(a.lanes_per_pair64 ? a.lanes_per_pair64 : 32)) / 64;
+  want = std::max<uint64_t>(want, kThreads);
+  const uint64_t blocks = (want + kThreads - 1) / kThreads;
   const unsigned grid = static_cast<unsigned>(std::min<uint64_t>(blocks, uint64_t(g)));
   lane_pipeline_kernel<L><<<grid, kThreads, smem, stream>>>(a);
   CUBFF_CUDA_TRY(cudaGetLastError());
