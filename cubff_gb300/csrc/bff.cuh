@@ -14,7 +14,13 @@
 //  * '[' / ']' masks (built on the first loop command) let bracket matching
 //    walk only bracket positions;
 //  * masks are patched on writes that change a byte's op;
-//  * exact cycle fast-forward at backward jumps (cycle.cuh).
+//  * exact cycle fast-forward at backward jumps (cycle.cuh), extended to
+//    head drift: a head that no command used as an address since the
+//    snapshot may differ from the snapshot's.  Control flow depends only on
+//    pc, the used heads and the tape, so the segment since the snapshot
+//    repeats with that head shifted by the same amount each time; k
+//    repetitions advance i by k*P, nskip by k times the segment's skips and
+//    the head by k times its shift (mod 128).
 #pragma once
 
 #include "cycle.cuh"
@@ -29,8 +35,11 @@ struct BffMachine {
   int pc, h0, h1;
   uint32_t i, nskip, mods;
   bool have_brk;
+  bool used0, used1;  // heads used as addresses since the snapshot
   Mask128 cmd, opn, cls;
-  CycleSnap snap;
+  // Brent-schedule snapshot taken at a backward jump.
+  int s_pc, s_h0, s_h1;
+  uint32_t s_mods, s_i, s_skip, s_power, s_lam;
 
   // cmd_mask: bit p set iff tape byte p is a command (op < kNull).
   __host__ __device__ __forceinline__ void begin(const LaneBytes t, Mask128 cmd_mask) {
@@ -45,7 +54,35 @@ struct BffMachine {
       pc = 0;
     }
     i = nskip = mods = 0;
-    snap = CycleSnap();
+    used0 = used1 = false;
+    s_pc = -1;
+    s_h0 = s_h1 = 0;
+    s_mods = s_i = s_skip = 0;
+    s_power = 1;
+    s_lam = 0;
+  }
+
+  // At a step boundary right after a backward jump.
+  __host__ __device__ __forceinline__ void visit() {
+    if (pc == s_pc && mods == s_mods && (!used0 || h0 == s_h0) && (!used1 || h1 == s_h1)) {
+      const uint32_t period = i - s_i;
+      const uint32_t k = (kStepLimit - i) / period;
+      i += k * period;
+      nskip += k * (nskip - s_skip);
+      h0 = (h0 + static_cast<int>(k) * (h0 - s_h0)) & (kPair - 1);
+      h1 = (h1 + static_cast<int>(k) * (h1 - s_h1)) & (kPair - 1);
+    }
+    if (++s_lam == s_power) {
+      s_pc = pc;
+      s_h0 = h0;
+      s_h1 = h1;
+      s_mods = mods;
+      s_i = i;
+      s_skip = nskip;
+      s_power <<= 1;
+      s_lam = 0;
+      used0 = used1 = false;
+    }
   }
 
   __host__ __device__ __forceinline__ void build_brackets(const LaneBytes t,
@@ -103,14 +140,19 @@ struct BffMachine {
       case kInc0: h0 = (h0 + 1) & (kPair - 1); break;
       case kDec1: h1 = (h1 - 1) & (kPair - 1); break;
       case kInc1: h1 = (h1 + 1) & (kPair - 1); break;
-      case kPlus: { const uint32_t o = t.get(h0); write(t, optab, h0, o, o + 1); break; }
-      case kMinus: { const uint32_t o = t.get(h0); write(t, optab, h0, o, o - 1); break; }
-      case kCopy01: write(t, optab, h1, t.get(h1), t.get(h0)); break;
+      case kPlus: { used0 = true; const uint32_t o = t.get(h0); write(t, optab, h0, o, o + 1); break; }
+      case kMinus: { used0 = true; const uint32_t o = t.get(h0); write(t, optab, h0, o, o - 1); break; }
+      case kCopy01:
+        used0 = used1 = true;
+        write(t, optab, h1, t.get(h1), t.get(h0));
+        break;
       case kCopy10:
+        used0 = used1 = true;
         write(t, optab, h0, t.get(h0), t.get(h1));
         if (kLogic == kLogicSelfmove) h1 = (h1 + 1) & (kPair - 1);
         break;
       case kLoopStart:
+        used0 = true;
         if ((t.get(h0) & kNullMask) == 0) {
           if (kLogic == kLogicJump8) {
             pc += 8;
@@ -129,6 +171,7 @@ struct BffMachine {
         }
         break;
       case kLoopEnd:
+        used0 = true;
         if ((t.get(h0) & kNullMask) != 0) {
           back = true;
           if (kLogic == kLogicJump8) {
@@ -155,7 +198,7 @@ struct BffMachine {
     pc++;
     if (pc >= kPair || i >= kStepLimit) return true;
     if (back) {
-      i += snap.visit(pc, h0, h1, mods, i, &nskip, kStepLimit);
+      visit();
       if (i >= kStepLimit) return true;
     }
     return false;

@@ -110,7 +110,9 @@ int cubff_soup::ensure_buffers() {
     CUBFF_CUDA_TRY(cudaMalloc(&d_counters, kCounterWords * sizeof(unsigned long long)));
     CUBFF_CUDA_TRY(cudaMallocHost(&h_counters, kCounterWords * sizeof(unsigned long long)));
     CUBFF_CUDA_TRY(cudaMalloc(&d_mutmask, size_t(batch) * (p.num_programs / 2) * sizeof(uint4)));
-    CUBFF_CUDA_TRY(cudaMalloc(&d_ver, p.num_programs * sizeof(uint32_t)));
+    CUBFF_CUDA_TRY(cudaMalloc(&d_inv, size_t(batch) * p.num_programs * sizeof(uint32_t)));
+    CUBFF_CUDA_TRY(cudaMalloc(&d_readycnt, size_t(batch) * (p.num_programs / 2) * sizeof(uint32_t)));
+    CUBFF_CUDA_TRY(cudaMalloc(&d_queue, size_t(batch) * (p.num_programs / 2) * sizeof(uint32_t)));
     CUBFF_CUDA_TRY(cudaMalloc(&d_ctl, 4 * sizeof(uint32_t)));
     CUBFF_CUDA_TRY(cudaMemset(d_ctl, 0, 4 * sizeof(uint32_t)));
     CUBFF_CUDA_TRY(cudaMallocHost(&h_ctl, 4 * sizeof(uint32_t)));
@@ -129,12 +131,14 @@ void cubff_soup::release() {
   if (d_counters) cudaFree(d_counters);
   if (h_counters) cudaFreeHost(h_counters);
   if (h_pat_perm) cudaFreeHost(h_pat_perm);
-  if (d_ver) cudaFree(d_ver);
+  if (d_inv) cudaFree(d_inv);
+  if (d_readycnt) cudaFree(d_readycnt);
+  if (d_queue) cudaFree(d_queue);
+  d_inv = d_readycnt = d_queue = nullptr;
   if (d_mutmask) cudaFree(d_mutmask);
   d_mutmask = nullptr;
   if (d_ctl) cudaFree(d_ctl);
   if (h_ctl) cudaFreeHost(h_ctl);
-  d_ver = nullptr;
   d_ctl = nullptr;
   h_ctl = nullptr;
   d_soup = nullptr;
@@ -193,6 +197,7 @@ int cubff_soup::fill_pairing(uint64_t first, uint32_t count) {
       return set_error(CUBFF_EINVAL, "unknown pairing mode %d", p.pairing);
   }
   CUBFF_TRY(launch_mutation_masks(s0, first, count, n, p.mutation_prob, d_mutmask, st));
+  CUBFF_TRY(launch_inverse(d_perm, count, n, d_inv, st));
   perm_first = first;
   perm_count = count;
   return CUBFF_OK;
@@ -236,8 +241,9 @@ int cubff_soup::run(uint64_t n_epochs, uint64_t *ops_out, uint64_t *raw_out, uin
         seg = std::min<uint64_t>(seg, r - e + 1);
       }
       const uint64_t slot = e - perm_first;
-      CUBFF_CUDA_TRY(cudaMemsetAsync(d_ver, 0, n * sizeof(uint32_t), st));
-      CUBFF_CUDA_TRY(cudaMemsetAsync(d_ctl, 0, 2 * sizeof(uint32_t), st));  // task counter
+      CUBFF_CUDA_TRY(cudaMemsetAsync(d_readycnt, 0, seg * (n / 2) * sizeof(uint32_t), st));
+      CUBFF_CUDA_TRY(cudaMemsetAsync(d_queue, 0, seg * (n / 2) * sizeof(uint32_t), st));
+      CUBFF_CUDA_TRY(cudaMemsetAsync(d_ctl, 0, 2 * sizeof(uint32_t), st));  // queue head, tail
       PipeArgs a;
       a.soup = d_soup;
       a.perm = d_perm + slot * n;
@@ -248,8 +254,10 @@ int cubff_soup::run(uint64_t n_epochs, uint64_t *ops_out, uint64_t *raw_out, uin
       a.mutation_prob = p.mutation_prob;
       a.d_num_indices = p.pairing == CUBFF_PAIR_PATTERN ? d_num_indices + slot : nullptr;
       a.mutmask = d_mutmask + slot * (n / 2);
-      a.ver = d_ver;
-      a.task_counter = reinterpret_cast<unsigned long long *>(d_ctl);
+      a.inv = d_inv + slot * n;
+      a.readycnt = d_readycnt;
+      a.queue = d_queue;
+      a.qctl = d_ctl;
       a.error = reinterpret_cast<int *>(d_ctl + 2);
       a.ops = d_counters + size_t(2) * kPipeCountSlots * c;
       a.lanes_per_pair64 = eng->lanes_per_pair64;

@@ -40,9 +40,11 @@ struct cubff_soup {
   size_t scratch_bytes = 0;
   uint64_t *h_pat_perm = nullptr;  // pinned staging for host pattern pairings
 
-  // Pipelined runs (pipeline.cu): per-program epoch versions, and the chunk
-  // counter + error flag of the current launch.
-  uint32_t *d_ver = nullptr;
+  // Pipelined runs (pipeline.cu): ready-queue state, and the queue head/tail +
+  // error flag of the current launch (d_ctl).
+  uint32_t *d_inv = nullptr;       // [batch][num_programs] inverse shuffles
+  uint32_t *d_readycnt = nullptr;  // [batch][num_programs / 2] ready-queue input counts
+  uint32_t *d_queue = nullptr;     // [batch][num_programs / 2] ready queue
   uint4 *d_mutmask = nullptr;  // [batch][num_programs / 2] mutation masks
   uint32_t *d_ctl = nullptr;
   uint32_t *h_ctl = nullptr;

@@ -55,11 +55,13 @@ struct PipeArgs {
   uint32_t mutation_prob;
   const uint64_t *d_num_indices;        // [n_epochs] or nullptr (= n / 2)
   const uint4 *mutmask;                 // [n_epochs][n / 2] mutation masks
-  uint32_t *ver;                        // [n] epochs completed per program, zeroed
-  unsigned long long *task_counter;     // zeroed
+  const uint32_t *inv;                  // [n_epochs][n] position of program p in perm
+  uint32_t *readycnt;                   // [n_epochs][n / 2] inputs published, zeroed
+  uint32_t *queue;                      // [(n_epochs - 1) * n / 2] ready tasks + 1, zeroed
+  uint32_t *qctl;                       // [0] head, [1] tail; zeroed
   int *error;                           // set when a bounded wait gives up
   unsigned long long *ops;              // [n_epochs][kCountSlots][2]: ops, raw
-  uint32_t lanes_per_pair64;            // lanes in flight per 64 pairs (0 = default)
+  uint32_t lanes_per_pair64;            // lanes per 64 pairs of an epoch (0 = default)
 };
 constexpr int kPipeCountSlots = 32;
 
@@ -67,6 +69,8 @@ constexpr int kPipeCountSlots = 32;
 int launch_pipeline(int lang, const PipeArgs &a, int device, cudaStream_t stream);
 int launch_mutation_masks(uint64_t s0, uint64_t e0, uint32_t n_epochs, uint64_t n, uint32_t prob,
                           uint4 *out, cudaStream_t stream);
+int launch_inverse(const uint32_t *perm, uint32_t n_epochs, uint64_t n, uint32_t *inv,
+                   cudaStream_t stream);
 int launch_epoch(int lang, const EpochArgs &a, cudaStream_t stream);
 int launch_init(uint64_t key, uint64_t n, uint8_t *soup, int zero_init,
                 uint64_t count, cudaStream_t stream);

@@ -173,6 +173,14 @@ __global__ void cyclic_kernel(uint64_t first_epoch, uint64_t n, uint64_t m, uint
                           : static_cast<uint32_t>(i == 0 ? n - 1 : i - 1);
 }
 
+// inv[e][perm[e][i]] = i: the position of each program in an epoch's shuffle.
+__global__ void inverse_kernel(const uint32_t *perm, uint64_t n, uint64_t m, uint32_t *inv) {
+  const uint64_t idx = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (idx >= m) return;
+  const uint64_t e = idx / n;
+  inv[e * n + perm[idx]] = static_cast<uint32_t>(idx - e * n);
+}
+
 unsigned blocks_for(uint64_t m, unsigned t) { return static_cast<unsigned>((m + t - 1) / t); }
 
 }  // namespace
@@ -193,6 +201,15 @@ int launch_shuffle(uint64_t s0, uint64_t first_epoch, uint32_t E, uint64_t n,
   fy_link<<<blocks_for(m, 256), 256, 0, stream>>>(n, m, b.j, b.cnt, b.start, b.bucket,
                                                   b.nxt, b.par);
   fy_resolve<<<blocks_for(m, 256), 256, 0, stream>>>(n, m, b.j, b.nxt, b.par, out);
+  CUBFF_CUDA_TRY(cudaGetLastError());
+  return CUBFF_OK;
+}
+
+int launch_inverse(const uint32_t *perm, uint32_t E, uint64_t n, uint32_t *inv,
+                   cudaStream_t stream) {
+  const uint64_t m = n * E;
+  if (m == 0) return CUBFF_OK;
+  inverse_kernel<<<blocks_for(m, 256), 256, 0, stream>>>(perm, n, m, inv);
   CUBFF_CUDA_TRY(cudaGetLastError());
   return CUBFF_OK;
 }

@@ -96,23 +96,37 @@ __global__ void mutation_mask_kernel(uint64_t s0, uint64_t e0, uint64_t npairs, 
 }
 
 constexpr int kCountSlots = kPipeCountSlots;  // per-epoch counter slots (spread the atomics)
-constexpr int kStepsPerVisit = 4;
+constexpr int kStepsPerVisit = 8;
+constexpr int kStepsLong = 64;
+constexpr uint32_t kLongRaw = 256;
 
-// Lane-level dataflow.  Every lane runs pairs one after another; a pair
-// depends only on the two pairs of the previous epoch that wrote its
-// programs.  Tasks (epoch-major pair order) are dealt out in blocks of 32:
-// warp w owns blocks w, w + W, w + 2W, ... (W = warps in the grid) and its
-// lanes take the block's tasks in order as they become idle.  The lowest
-// unfinished task is always runnable and either held by its owner warp or
-// about to be taken by one of its idle lanes, so the pipeline cannot
-// deadlock.
+// Ready-queue dataflow.  A pair of epoch e+1 can run once the two pairs of
+// epoch e that wrote its programs are done.  A finished pair notifies the
+// consumers of its two programs (inv gives a program's position in the next
+// epoch's shuffle, hence its pair); the second notification of a consumer
+// pushes it into the ready queue.  Warps claim queue slots in bulk, so the
+// lanes they hand out stage their pairs together; epoch-0 pairs of the run
+// are implicitly ready (slots [0, npairs)).  Every pushed task is runnable,
+// so no lane ever waits on a dependency; a lane only waits for a claimed
+// slot to be filled, and every slot below the task count is eventually
+// filled (all pairs of epoch e complete => all of epoch e+1 are pushed).
 //
-// No global access is consumed in the iteration that issues it: the next
-// block's shuffle indices are loaded one block ahead, version polls are
-// relaxed loads read back in the following iteration (with an acquire fence
-// once a pair is ready), and a ready pair's gather lands in registers that
-// are staged into shared memory in the following iteration.  Lane states:
-// idle -> wait -> stage -> run -> (write back, publish) -> idle.
+// No global access is consumed in the iteration that issues it where that
+// can be avoided: queue entries, shuffle indices and gathers land in
+// registers read back in a later iteration.  Lane states:
+//   idle -> slot (wait for the entry) -> index -> stage -> run -> notify -> idle.
+constexpr int kClaimMin = 8;
+
+__device__ __forceinline__ uint32_t atom_add_acq_rel(uint32_t *p, uint32_t v) {
+  uint32_t old;
+  asm volatile("atom.acq_rel.gpu.global.add.u32 %0, [%1], %2;" : "=r"(old) : "l"(p), "r"(v) : "memory");
+  return old;
+}
+
+__device__ __forceinline__ void st_release_u32(uint32_t *p, uint32_t v) {
+  asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
 template <int L>
 __global__ void __launch_bounds__(kThreads) lane_pipeline_kernel(PipeArgs a) {
   extern __shared__ __align__(16) uint8_t smem[];
@@ -130,73 +144,104 @@ __global__ void __launch_bounds__(kThreads) lane_pipeline_kernel(PipeArgs a) {
   __syncthreads();  // tables are read-only from here on; warps run independently
   const LaneBytes t{smem, lane_base(tid)};
   const LaneBytes stk{smem + kGroups * kGroupBytes, lane_base(tid)};
-  const uint64_t npairs = a.n / 2;
-  const uint64_t total = npairs * a.n_epochs;
+  const uint32_t npairs = static_cast<uint32_t>(a.n / 2);
+  const uint32_t n_ep = a.n_epochs;
+  const uint32_t total = npairs * n_ep;
   const uint64_t warp_id = uint64_t(blockIdx.x) * (kThreads / 32) + (tid >> 5);
-  const uint64_t n_warps = uint64_t(gridDim.x) * (kThreads / 32);
-  const uint32_t slot = static_cast<uint32_t>(warp_id % kCountSlots);
+  const uint32_t slot_ctr = static_cast<uint32_t>(warp_id % kCountSlots);
   const uint32_t lt_mask = (1u << lane) - 1;
 
-  // Shuffle-index pair (p1 | p2 << 32) of task `task`, or 0 past the end.
-  auto load_qp = [&](uint64_t task) -> uint64_t {
-    if (task >= total) return 0;
-    const uint64_t e = task / npairs, k = task - e * npairs;
-    return *reinterpret_cast<const unsigned long long *>(a.perm + e * a.n + 2 * k);
-  };
-  uint64_t cur_block = warp_id, next_block = warp_id + n_warps;
-  uint64_t cur_qp = load_qp(cur_block * 32 + lane);
-  uint64_t next_qp = load_qp(next_block * 32 + lane);
-  uint32_t used = 0;  // tasks of the current block already taken
-
-  enum : uint32_t { kIdle = 0, kWait = 1, kStage = 2, kRun = 3, kDone = 4 };
-  uint32_t state = kIdle, e = 0, p1 = 0, p2 = 0, v1 = 0, v2 = 0;
-  uint64_t k = 0, t_wait = 0;
-  uint32_t poll_gap = 1, poll_in = 0;  // per-lane poll backoff (iterations)
-  uint32_t err = 0;                    // error flag as of the last poll
+  enum : uint32_t { kIdle, kSlot, kIndex, kStage, kRun, kNotify, kDone };
+  uint32_t state = kIdle, slot = 0, task = 0, e = 0, k = 0, p1 = 0, p2 = 0;
+  uint32_t qv = 0, poll_gap = 1, poll_in = 0, err = 0;
+  uint32_t j1 = 0, j2 = 0, c1 = 0, c2 = 0;
+  uint64_t qp = 0, t_wait = 0;
   bool dirty = false, evaluated = false;
   uint4 g[8];
   uint4 mm = make_uint4(0, 0, 0, 0);
   LaneMachine<L> m;
 
   while (true) {
-    // 1. Idle lanes take the next tasks of the warp's blocks.
+    // 1. Bulk claim of queue slots by idle lanes.
     const uint32_t idle = __ballot_sync(0xffffffffu, state == kIdle);
-    if (idle) {
-      const uint32_t idx = used + __popc(idle & lt_mask);
-      const uint64_t qa = __shfl_sync(0xffffffffu, cur_qp, idx & 31);
-      const uint64_t qb = __shfl_sync(0xffffffffu, next_qp, idx & 31);
+    const uint32_t busy = __ballot_sync(0xffffffffu, state != kIdle && state != kDone);
+    if (idle && (__popc(idle) >= kClaimMin || busy == 0)) {
+      const int leader = __ffs(idle) - 1;
+      uint32_t base = 0;
+      if (lane == static_cast<uint32_t>(leader)) base = atomicAdd(a.qctl, __popc(idle));
+      base = __shfl_sync(0xffffffffu, base, leader);
       if (state == kIdle) {
-        const uint64_t task = idx < 32 ? cur_block * 32 + idx : next_block * 32 + (idx - 32);
-        if (task >= total) {
+        slot = base + __popc(idle & lt_mask);
+        if (slot >= total) {
           state = kDone;
+        } else if (slot < npairs) {  // an epoch-0 pair of the run: ready
+          task = slot;
+          state = kIndex;
+          qp = *reinterpret_cast<const unsigned long long *>(a.perm + 2 * uint64_t(task));
         } else {
-          e = static_cast<uint32_t>(task / npairs);
-          k = task - uint64_t(e) * npairs;
-          const uint64_t qp = idx < 32 ? qa : qb;
-          p1 = static_cast<uint32_t>(qp);
-          p2 = static_cast<uint32_t>(qp >> 32);
-          v1 = ld_relaxed(a.ver + p1);
-          v2 = ld_relaxed(a.ver + p2);
-          state = kWait;
-          t_wait = 0;
+          state = kSlot;
+          qv = ld_relaxed(a.queue + (slot - npairs));
           poll_gap = 1;
           poll_in = 0;
+          t_wait = 0;
         }
-      }
-      used += __popc(idle);
-      if (used >= 32) {  // current block exhausted: advance, prefetch the next
-        used -= 32;
-        cur_block = next_block;
-        cur_qp = next_qp;
-        next_block += n_warps;
-        next_qp = load_qp(next_block * 32 + lane);
       }
     }
     if (__all_sync(0xffffffffu, state == kDone)) break;
     bool progressed = false;
 
-    // 2. Staging: the gather issued in an earlier iteration has landed.
-    if (state == kStage) {
+    if (state == kSlot) {
+      // 2. Waiting for the claimed slot's entry (polled in an earlier iteration).
+      if (qv != 0) {
+        task = qv - 1;
+        e = task / npairs;
+        qp = *reinterpret_cast<const unsigned long long *>(
+            a.perm + uint64_t(e) * a.n + 2 * uint64_t(task - e * npairs));
+        state = kIndex;
+        progressed = true;
+      } else if (poll_in-- == 0) {
+        if (err) {
+          state = kDone;
+        } else {
+          const uint64_t now = globaltimer_ns();
+          if (t_wait == 0) {
+            t_wait = now;
+          } else if (now - t_wait > kWaitLimitNs) {
+            atomicExch(a.error, 1);
+            state = kDone;
+          }
+        }
+        if (state == kSlot) {
+          qv = ld_relaxed(a.queue + (slot - npairs));
+          err = ld_relaxed(reinterpret_cast<const uint32_t *>(a.error));
+          poll_gap = poll_gap < 16 ? poll_gap * 2 : 16;
+          poll_in = poll_gap;
+        }
+      }
+    } else if (state == kIndex) {
+      // 3. Shuffle indices landed: order after the producers, issue the gather,
+      //    the mutation mask and the next epoch's positions of both programs.
+      e = task / npairs;
+      k = task - e * npairs;
+      p1 = static_cast<uint32_t>(qp);
+      p2 = static_cast<uint32_t>(qp >> 32);
+      fence_acq_rel_gpu();
+      const uint4 *g1 = reinterpret_cast<const uint4 *>(a.soup + uint64_t(p1) * kTape);
+      const uint4 *g2 = reinterpret_cast<const uint4 *>(a.soup + uint64_t(p2) * kTape);
+#pragma unroll
+      for (int q = 0; q < 4; q++) {
+        g[q] = __ldcg(g1 + q);
+        g[4 + q] = __ldcg(g2 + q);
+      }
+      mm = __ldg(a.mutmask + task);
+      if (e + 1 < n_ep) {
+        j1 = __ldg(a.inv + uint64_t(e + 1) * a.n + p1);
+        j2 = __ldg(a.inv + uint64_t(e + 1) * a.n + p2);
+      }
+      state = kStage;
+      progressed = true;
+    } else if (state == kStage) {
+      // 4. Stage the pair: bytes into shared memory, command mask, mutations.
       Mask128 cmd{0, 0};
 #pragma unroll
       for (int q = 0; q < 32; q++) {
@@ -233,47 +278,14 @@ __global__ void __launch_bounds__(kThreads) lane_pipeline_kernel(PipeArgs a) {
       m.begin(t, cmd);
       state = kRun;
       progressed = true;
-    } else if (state == kWait) {
-      // 3. Waiting: versions polled in the previous iteration.
-      if (v1 >= e && v2 >= e) {
-        fence_acq_rel_gpu();  // order the gather after the observed releases
-        const uint4 *g1 = reinterpret_cast<const uint4 *>(a.soup + uint64_t(p1) * kTape);
-        const uint4 *g2 = reinterpret_cast<const uint4 *>(a.soup + uint64_t(p2) * kTape);
-#pragma unroll
-        for (int q = 0; q < 4; q++) {
-          g[q] = __ldcg(g1 + q);
-          g[4 + q] = __ldcg(g2 + q);
-        }
-        mm = __ldg(a.mutmask + uint64_t(e) * npairs + k);
-        state = kStage;
-        progressed = true;
-      } else if (poll_in-- == 0) {
-        // Not ready: the error flag and the deadline are checked on the poll
-        // schedule, and the next poll is issued (read back next time).
-        if (err) {
-          state = kDone;
-        } else {
-          const uint64_t now = globaltimer_ns();
-          if (t_wait == 0) {
-            t_wait = now;
-          } else if (now - t_wait > kWaitLimitNs) {
-            atomicExch(a.error, 1);
-            state = kDone;
-          }
-        }
-        if (state == kWait) {
-          v1 = ld_relaxed(a.ver + p1);
-          v2 = ld_relaxed(a.ver + p2);
-          err = ld_relaxed(reinterpret_cast<const uint32_t *>(a.error));
-          poll_gap = poll_gap < 16 ? poll_gap * 2 : 16;
-          poll_in = poll_gap;
-        }
-      }
     } else if (state == kRun) {
-      // 4. Running: a few interpreter steps; finish with write-back + publish.
+      // 5. A few interpreter steps; on the end, write back and notify.
       progressed = true;
       bool fin = !evaluated;
-      for (int r = 0; r < kStepsPerVisit && !fin; r++) fin = m.step(t, stk, optab);
+      // Pairs that have run long are the ones later epochs wait on: give
+      // them more steps per visit of the warp.
+      const int steps = m.raw() > kLongRaw ? kStepsLong : kStepsPerVisit;
+      for (int r = 0; r < steps && !fin; r++) fin = m.step(t, stk, optab);
       if (fin) {
         if (dirty || (evaluated && m.mods() != 0)) {
           uint32_t w[32];
@@ -292,16 +304,43 @@ __global__ void __launch_bounds__(kThreads) lane_pipeline_kernel(PipeArgs a) {
             o2[q] = make_uint4(w[16 + 4 * q], w[16 + 4 * q + 1], w[16 + 4 * q + 2],
                                w[16 + 4 * q + 3]);
         }
-        st_release(a.ver + p1, e + 1);  // orders the tape stores before the flags
-        st_release(a.ver + p2, e + 1);
         if (evaluated) {
-          unsigned long long *c = a.ops + (uint64_t(e) * kCountSlots + slot) * 2;
+          unsigned long long *c = a.ops + (uint64_t(e) * kCountSlots + slot_ctr) * 2;
           if (m.ops()) atomicAdd(c, static_cast<unsigned long long>(m.ops()));
           if (m.raw()) atomicAdd(c + 1, static_cast<unsigned long long>(m.raw()));
         }
-        state = kIdle;
+        if (e + 1 < n_ep) {
+          // The acq_rel increments order the stores above before them, and
+          // make the earlier producer's stores visible to whoever pushes.
+          uint32_t *rc = a.readycnt + uint64_t(e + 1) * npairs;
+          c1 = atom_add_acq_rel(rc + (j1 >> 1), 1);
+          c2 = atom_add_acq_rel(rc + (j2 >> 1), 1);
+          state = kNotify;
+        } else {
+          state = kIdle;
+        }
       }
     }
+    // 6. Push the consumers whose second input this pair was.
+    const bool push1 = state == kNotify && c1 == 1;
+    const bool push2 = state == kNotify && c2 == 1 && (j2 >> 1) != (j1 >> 1);
+    const bool push1b = state == kNotify && c2 == 1 && (j2 >> 1) == (j1 >> 1);
+    const uint32_t nmask1 = __ballot_sync(0xffffffffu, push1 || push1b);
+    const uint32_t nmask2 = __ballot_sync(0xffffffffu, push2);
+    if (nmask1 | nmask2) {
+      const int leader = __ffs(nmask1 | nmask2) - 1;
+      uint32_t base = 0;
+      if (lane == static_cast<uint32_t>(leader))
+        base = atomicAdd(a.qctl + 1, __popc(nmask1) + __popc(nmask2));
+      base = __shfl_sync(0xffffffffu, base, leader);
+      const uint32_t next = (e + 1) * npairs;
+      if (push1 || push1b)
+        st_release_u32(a.queue + base + __popc(nmask1 & lt_mask), next + (j1 >> 1) + 1);
+      if (push2)
+        st_release_u32(a.queue + base + __popc(nmask1) + __popc(nmask2 & lt_mask),
+                       next + (j2 >> 1) + 1);
+    }
+    if (state == kNotify) state = kIdle;
     if (!__any_sync(0xffffffffu, progressed)) __nanosleep(200);
   }
 }

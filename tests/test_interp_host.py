@@ -81,8 +81,18 @@ def test_interpreter_matches_oracle(host_lib, lang):
 CRAFTED = {
     # no-write infinite loop: fast-forwarded to the step limit
     "bff_noheads": [b"[" + b"a" * 40 + b"]", b"+[]", b"+[<>]", b"+[>]", b"+[>+<-]",
-                    b"]]]]", b"[[[[", b"+[[]]", b"-[-]+[" + b"z" * 100 + b"]"],
-    "bff": [b"\x05\x07+[<>]", b"\x00\x00+[{}]", b"\x01\x02+[.,]"],
+                    b"]]]]", b"[[[[", b"+[[]]", b"-[-]+[" + b"z" * 100 + b"]",
+                    # head-1 drift loops (h1 moves, never used as an address)
+                    b"+[}]", b"+[{{}" + b"q" * 30 + b"]", b"+[}}}" + b"q" * 60 + b"]",
+                    b"+[}.]", b"+[},]", b"+[}" + b"q" * 50 + b"{{]",
+                    # a tape that ran 6241 loop iterations of an h1-drift loop
+                    bytes.fromhex(
+                        "515b7d7b7b7d7d7b807d7d197b7d7d7b7b7d7d7b7b7d7d7b7b7dba7b7b7d7d7b7b7d7d"
+                        "7b2a8b57fefec3f55d7ea5d2060d7452717c802acd73518f415483763c58bf7dcea689"
+                        "2513bf6f3e70691e6f2477001865ebc883a21e54783b8dd1708cb559afcda34ac30191"
+                        "81742074a43a347c6f575c5f9c09181259f3389b9b507b")],
+    "bff": [b"\x05\x07+[<>]", b"\x00\x00+[{}]", b"\x01\x02+[.,]", b"\x05\x07+[}]",
+            b"\x05\x07+[}" + b"q" * 40 + b"]", b"\x05\x07+[}]" + b"+" * 10],
     "bff8": [b"\x05\x07+" + b"a" * 5 + b"]", b"\x05\x07" + b"]" * 8],
     "forth": [bytes([0x41, 0x04, 0x05, 0xC3]), bytes([0x20, 0xC1]), bytes([0x41, 0xC0]),
               bytes([0x40, 0x07, 0xC2])],
