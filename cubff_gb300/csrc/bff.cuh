@@ -14,10 +14,14 @@
 //  * '[' / ']' masks (built on the first loop command) let bracket matching
 //    walk only bracket positions;
 //  * masks are patched on writes that change a byte's op;
-//  * exact cycle fast-forward at backward jumps (cycle.cuh), extended to
-//    head drift: a head that no command used as an address since the
-//    snapshot may differ from the snapshot's.  Control flow depends only on
-//    pc, the used heads and the tape, so the segment since the snapshot
+//  * exact cycle fast-forward at backward jumps (cycle.cuh): the state is
+//    (pc, heads, tape).  Tape equality with the snapshot is checked on the
+//    positions written since the snapshot only: the first write to a
+//    position saves its snapshot value in a second per-lane area (the stack
+//    area, unused by BFF), so loops whose writes cancel are caught too.
+//    Head drift is allowed: a head that no command used as an address since
+//    the snapshot may differ from the snapshot's.  Control flow depends only
+//    on pc, the used heads and the tape, so the segment since the snapshot
 //    repeats with that head shifted by the same amount each time; k
 //    repetitions advance i by k*P, nskip by k times the segment's skips and
 //    the head by k times its shift (mod 128).
@@ -37,6 +41,7 @@ struct BffMachine {
   bool have_brk;
   bool used0, used1;  // heads used as addresses since the snapshot
   Mask128 cmd, opn, cls;
+  Mask128 touched;    // positions written since the snapshot
   // Brent-schedule snapshot taken at a backward jump.
   int s_pc, s_h0, s_h1;
   uint32_t s_mods, s_i, s_skip, s_power, s_lam;
@@ -55,6 +60,7 @@ struct BffMachine {
     }
     i = nskip = mods = 0;
     used0 = used1 = false;
+    touched = Mask128{0, 0};
     s_pc = -1;
     s_h0 = s_h1 = 0;
     s_mods = s_i = s_skip = 0;
@@ -62,9 +68,27 @@ struct BffMachine {
     s_lam = 0;
   }
 
+  // True when every position written since the snapshot holds its snapshot
+  // value again (saved in snapa by the first write).
+  __host__ __device__ __forceinline__ bool tape_back(const LaneBytes t, const LaneBytes snapa) const {
+    if (mods == s_mods) return true;
+    uint64_t lo = touched.lo, hi = touched.hi;
+    while (lo) {
+      const int p = ffs64(lo) - 1;
+      lo &= lo - 1;
+      if (t.get(p) != snapa.get(p)) return false;
+    }
+    while (hi) {
+      const int p = 63 + ffs64(hi);
+      hi &= hi - 1;
+      if (t.get(p) != snapa.get(p)) return false;
+    }
+    return true;
+  }
+
   // At a step boundary right after a backward jump.
-  __host__ __device__ __forceinline__ void visit() {
-    if (pc == s_pc && mods == s_mods && (!used0 || h0 == s_h0) && (!used1 || h1 == s_h1)) {
+  __host__ __device__ __forceinline__ void visit(const LaneBytes t, const LaneBytes snapa) {
+    if (pc == s_pc && (!used0 || h0 == s_h0) && (!used1 || h1 == s_h1) && tape_back(t, snapa)) {
       const uint32_t period = i - s_i;
       const uint32_t k = (kStepLimit - i) / period;
       i += k * period;
@@ -82,6 +106,7 @@ struct BffMachine {
       s_power <<= 1;
       s_lam = 0;
       used0 = used1 = false;
+      touched = Mask128{0, 0};
     }
   }
 
@@ -99,13 +124,17 @@ struct BffMachine {
   }
 
   // Writes tape[a] = v (old value o); patches the masks when the op changes.
-  __host__ __device__ __forceinline__ void write(const LaneBytes t,
+  __host__ __device__ __forceinline__ void write(const LaneBytes t, const LaneBytes snapa,
                                                  const uint8_t *__restrict__ optab, int a,
                                                  uint32_t o, uint32_t v) {
     v &= 0xFF;
     if (v == o) return;
     t.set(a, v);
     mods++;
+    if (!mask_test(touched, a)) {
+      mask_assign(touched, a, true);
+      snapa.set(a, o);
+    }
     const uint32_t co = optab[o], cn = optab[v];
     if (co != cn) {
       mask_assign(cmd, a, cn < kNull);
@@ -118,7 +147,7 @@ struct BffMachine {
 
   // One step: a run of no-ops (if any) and then one command.  Returns true
   // when the program has ended; the op count is then i - nskip.
-  __host__ __device__ __forceinline__ bool step(const LaneBytes t,
+  __host__ __device__ __forceinline__ bool step(const LaneBytes t, const LaneBytes snapa,
                                                 const uint8_t *__restrict__ optab) {
     const int q = mask_next(cmd, pc);
     const uint32_t run = static_cast<uint32_t>(q - pc);
@@ -140,15 +169,15 @@ struct BffMachine {
       case kInc0: h0 = (h0 + 1) & (kPair - 1); break;
       case kDec1: h1 = (h1 - 1) & (kPair - 1); break;
       case kInc1: h1 = (h1 + 1) & (kPair - 1); break;
-      case kPlus: { used0 = true; const uint32_t o = t.get(h0); write(t, optab, h0, o, o + 1); break; }
-      case kMinus: { used0 = true; const uint32_t o = t.get(h0); write(t, optab, h0, o, o - 1); break; }
+      case kPlus: { used0 = true; const uint32_t o = t.get(h0); write(t, snapa, optab, h0, o, o + 1); break; }
+      case kMinus: { used0 = true; const uint32_t o = t.get(h0); write(t, snapa, optab, h0, o, o - 1); break; }
       case kCopy01:
         used0 = used1 = true;
-        write(t, optab, h1, t.get(h1), t.get(h0));
+        write(t, snapa, optab, h1, t.get(h1), t.get(h0));
         break;
       case kCopy10:
         used0 = used1 = true;
-        write(t, optab, h0, t.get(h0), t.get(h1));
+        write(t, snapa, optab, h0, t.get(h0), t.get(h1));
         if (kLogic == kLogicSelfmove) h1 = (h1 + 1) & (kPair - 1);
         break;
       case kLoopStart:
@@ -198,7 +227,7 @@ struct BffMachine {
     pc++;
     if (pc >= kPair || i >= kStepLimit) return true;
     if (back) {
-      visit();
+      visit(t, snapa);
       if (i >= kStepLimit) return true;
     }
     return false;
@@ -216,13 +245,14 @@ __host__ __device__ __forceinline__ Mask128 bff_command_mask(const LaneBytes t,
   return m;
 }
 
+// snapa: a second per-lane 128-byte area (snapshot values for the cycle check).
 template <bool kHeads, int kLogic, uint32_t kNullMask>
-__host__ __device__ __forceinline__ uint32_t bff_eval(const LaneBytes t,
+__host__ __device__ __forceinline__ uint32_t bff_eval(const LaneBytes t, const LaneBytes snapa,
                                                       const uint8_t *__restrict__ optab,
                                                       uint32_t *raw) {
   BffMachine<kHeads, kLogic, kNullMask> m;
   m.begin(t, bff_command_mask(t, optab));
-  while (!m.step(t, optab)) {
+  while (!m.step(t, snapa, optab)) {
   }
   *raw = m.raw();
   return m.ops();

@@ -45,8 +45,7 @@ __global__ void __launch_bounds__(kThreads) selfrep_kernel(const uint8_t *soup,
                                                            uint64_t n, uint64_t count,
                                                            uint64_t *result) {
   extern __shared__ __align__(16) uint8_t smem[];
-  constexpr bool kForthFam = LangTraits<L>::kForthFamily;
-  uint8_t *optab = smem + (kForthFam ? 2 : 1) * kGroups * kGroupBytes;
+  uint8_t *optab = smem + 2 * kGroups * kGroupBytes;
   const uint32_t tid = threadIdx.x;
   if (LangTraits<L>::kNeedsTable)
     for (uint32_t c = tid; c < 256; c += kThreads) optab[c] = op_of(L, c);

@@ -11,9 +11,11 @@ namespace cubff {
 constexpr int kThreads = 128;  // one group of four warps
 constexpr int kGroups = kThreads / 128;
 
+// Shared memory per CTA: two per-lane 128-byte areas per thread (the tape, and
+// the Forth stack or the BFF/SUBLEQ cycle-check snapshot), then the op table.
 template <int L>
 constexpr size_t epoch_smem_bytes() {
-  return (LangTraits<L>::kForthFamily ? 2 : 1) * kGroups * kGroupBytes + 256;
+  return 2 * kGroups * kGroupBytes + 256;
 }
 constexpr size_t kMaxEpochSmem = 2 * kGroups * kGroupBytes + 256;
 
@@ -49,8 +51,7 @@ __device__ __forceinline__ void mutate(uint64_t key0, uint32_t prob, uint32_t w[
 // threads converged and smem free for reuse after a __syncthreads().
 template <int L>
 __device__ __forceinline__ void epoch_cta(const EpochArgs &a, uint64_t block, uint8_t *smem) {
-  constexpr bool kForthFam = LangTraits<L>::kForthFamily;
-  uint8_t *optab = smem + (kForthFam ? 2 : 1) * kGroups * kGroupBytes;
+  uint8_t *optab = smem + 2 * kGroups * kGroupBytes;
   const uint32_t tid = threadIdx.x;
   if (LangTraits<L>::kNeedsTable)
     for (uint32_t c = tid; c < 256; c += kThreads) optab[c] = op_of(L, c);

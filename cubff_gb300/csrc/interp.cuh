@@ -26,17 +26,17 @@ template <int L>
 __host__ __device__ __forceinline__ uint32_t evaluate(const LaneBytes t, const LaneBytes stk,
                                              const uint8_t *__restrict__ optab,
                                              uint32_t *raw) {
-  if constexpr (L == kBff) return bff_eval<true, kLogicScan, 0xFF>(t, optab, raw);
-  else if constexpr (L == kBffNoheads) return bff_eval<false, kLogicScan, 0xFF>(t, optab, raw);
-  else if constexpr (L == kBffNoheads4bit) return bff_eval<false, kLogicScan, 0x0F>(t, optab, raw);
-  else if constexpr (L == kBffPerm) return bff_eval<true, kLogicScan, 0xFF>(t, optab, raw);
-  else if constexpr (L == kBff8) return bff_eval<true, kLogicJump8, 0xFF>(t, optab, raw);
-  else if constexpr (L == kBff8Noheads) return bff_eval<false, kLogicJump8, 0xFF>(t, optab, raw);
-  else if constexpr (L == kBffSelfmove) return bff_eval<true, kLogicSelfmove, 0xFF>(t, optab, raw);
+  if constexpr (L == kBff) return bff_eval<true, kLogicScan, 0xFF>(t, stk, optab, raw);
+  else if constexpr (L == kBffNoheads) return bff_eval<false, kLogicScan, 0xFF>(t, stk, optab, raw);
+  else if constexpr (L == kBffNoheads4bit) return bff_eval<false, kLogicScan, 0x0F>(t, stk, optab, raw);
+  else if constexpr (L == kBffPerm) return bff_eval<true, kLogicScan, 0xFF>(t, stk, optab, raw);
+  else if constexpr (L == kBff8) return bff_eval<true, kLogicJump8, 0xFF>(t, stk, optab, raw);
+  else if constexpr (L == kBff8Noheads) return bff_eval<false, kLogicJump8, 0xFF>(t, stk, optab, raw);
+  else if constexpr (L == kBffSelfmove) return bff_eval<true, kLogicSelfmove, 0xFF>(t, stk, optab, raw);
   else if constexpr (L == kForthtrivialReset) return forth_eval<true>(t, stk, optab, raw);
   else if constexpr (LangTraits<L>::kForthFamily) return forth_eval<false>(t, stk, optab, raw);
-  else if constexpr (L == kSubleq) return subleq_eval(t, raw);
-  else return rsubleq4_eval(t, raw);
+  else if constexpr (L == kSubleq) return subleq_eval(t, stk, raw);
+  else return rsubleq4_eval(t, stk, raw);
 }
 
 // A resumable interpreter of language L behind one interface (used by the
@@ -61,9 +61,9 @@ struct LaneMachine {
   }
   __host__ __device__ __forceinline__ bool step(const LaneBytes t, const LaneBytes stk,
                                                 const uint8_t *__restrict__ optab) {
-    if constexpr (L <= kBffSelfmove) return m.step(t, optab);
+    if constexpr (L <= kBffSelfmove) return m.step(t, stk, optab);
     else if constexpr (LangTraits<L>::kForthFamily) return m.step(t, stk, optab);
-    else return m.step(t);
+    else return m.step(t, stk);
   }
   __host__ __device__ __forceinline__ uint32_t ops() const { return m.ops(); }
   __host__ __device__ __forceinline__ uint32_t raw() const { return m.raw(); }

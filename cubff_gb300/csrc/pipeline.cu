@@ -130,9 +130,8 @@ __device__ __forceinline__ void st_release_u32(uint32_t *p, uint32_t v) {
 template <int L>
 __global__ void __launch_bounds__(kThreads) lane_pipeline_kernel(PipeArgs a) {
   extern __shared__ __align__(16) uint8_t smem[];
-  constexpr bool kForthFam = LangTraits<L>::kForthFamily;
   constexpr bool kBffFam = (L <= kBffSelfmove);
-  uint8_t *optab = smem + (kForthFam ? 2 : 1) * kGroups * kGroupBytes;
+  uint8_t *optab = smem + 2 * kGroups * kGroupBytes;
   uint8_t *cmdflag = optab + 256;
   const uint32_t tid = threadIdx.x, lane = tid & 31;
   if (LangTraits<L>::kNeedsTable) {
