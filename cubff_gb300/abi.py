@@ -41,6 +41,9 @@ SIGNATURES = {
     "cubff_shuffle_scratch_bytes": (sz, [u64, u32]),
     "cubff_shuffle_indices": (ci, [u64, u64, u32, u64, vp, vp, sz, vp]),
     "cubff_shuffle_indices_noalloc": (ci, [u64, u64, u32, u64, vp, vp]),
+    "cubff_run_epochs_workspace_bytes": (sz, [u64, u32]),
+    "cubff_run_epochs": (ci, [ci, vp, vp, vp, u64, u64, u32, u32, u64, vp, vp, sz, vp]),
+    "cubff_run_epochs_status": (ci, [vp, u64, u32, vp]),
     "cubff_engine_create": (ci, [ci, ctypes.POINTER(vp)]),
     "cubff_engine_destroy": (ci, [vp]),
     "cubff_soup_create": (ci, [vp, ctypes.POINTER(SoupParams), ctypes.POINTER(vp)]),

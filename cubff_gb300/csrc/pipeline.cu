@@ -417,3 +417,129 @@ int launch_pipeline(int lang, const PipeArgs &a, int device, cudaStream_t stream
 }
 
 }  // namespace cubff
+
+// ---------------------------------------------------------------------------
+// Kernel-level pipelined run on caller-owned buffers (cubff_run_epochs).
+
+namespace cubff {
+namespace {
+
+struct RunWs {
+  uint4 *mutmask;
+  uint32_t *inv, *readycnt, *queue, *ctl;
+  unsigned long long *counters;
+};
+
+size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
+
+RunWs run_ws(void *base, uint64_t n, uint32_t E) {
+  const uint64_t P = n / 2;
+  uint8_t *p = static_cast<uint8_t *>(base);
+  RunWs w;
+  w.mutmask = reinterpret_cast<uint4 *>(p);
+  p += align256(size_t(E) * P * sizeof(uint4));
+  w.inv = reinterpret_cast<uint32_t *>(p);
+  p += align256(size_t(E) * n * sizeof(uint32_t));
+  w.readycnt = reinterpret_cast<uint32_t *>(p);
+  p += align256(size_t(E) * P * sizeof(uint32_t));
+  w.queue = reinterpret_cast<uint32_t *>(p);
+  p += align256(size_t(E) * P * sizeof(uint32_t));
+  w.counters = reinterpret_cast<unsigned long long *>(p);
+  p += align256(size_t(E) * kPipeCountSlots * 2 * sizeof(unsigned long long));
+  w.ctl = reinterpret_cast<uint32_t *>(p);
+  return w;
+}
+
+// d_counts[e] += the per-slot counters of epoch e.
+__global__ void reduce_counts_kernel(const unsigned long long *slots, uint32_t E,
+                                     unsigned long long *out) {
+  const uint32_t e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= E) return;
+  unsigned long long o = 0, r = 0;
+  for (int s = 0; s < kPipeCountSlots; s++) {
+    o += slots[(uint64_t(e) * kPipeCountSlots + s) * 2];
+    r += slots[(uint64_t(e) * kPipeCountSlots + s) * 2 + 1];
+  }
+  out[2 * e] += o;
+  out[2 * e + 1] += r;
+}
+
+}  // namespace
+}  // namespace cubff
+
+extern "C" size_t cubff_run_epochs_workspace_bytes(uint64_t num_programs, uint32_t n_epochs) {
+  using namespace cubff;
+  const uint64_t P = num_programs / 2;
+  return align256(size_t(n_epochs) * P * sizeof(uint4)) +
+         align256(size_t(n_epochs) * num_programs * sizeof(uint32_t)) +
+         2 * align256(size_t(n_epochs) * P * sizeof(uint32_t)) +
+         align256(size_t(n_epochs) * kPipeCountSlots * 2 * sizeof(unsigned long long)) + 256;
+}
+
+extern "C" int cubff_run_epochs(int lang, uint8_t *d_programs, const uint32_t *d_shuf_idx,
+                                const uint64_t *d_num_indices, uint64_t params_seed,
+                                uint64_t first_epoch, uint32_t n_epochs, uint32_t mutation_prob,
+                                uint64_t num_programs, unsigned long long *d_counts,
+                                void *d_workspace, size_t workspace_bytes, void *stream) {
+  using namespace cubff;
+  if (lang < 0 || lang >= kNumLangs) return set_error(CUBFF_ENOTFOUND, "unknown language %d", lang);
+  if (!d_programs || !d_shuf_idx || !d_counts || !d_workspace || num_programs < 2 ||
+      num_programs % 2 != 0 || num_programs > (1ull << 31))
+    return set_error(CUBFF_EINVAL, "run_epochs: bad arguments");
+  if ((reinterpret_cast<uintptr_t>(d_programs) & 15) || (reinterpret_cast<uintptr_t>(d_shuf_idx) & 7) ||
+      (reinterpret_cast<uintptr_t>(d_workspace) & 255))
+    return set_error(CUBFF_EINVAL, "run_epochs: misaligned buffer (programs 16, indices 8, "
+                                   "workspace 256 bytes)");
+  if (workspace_bytes < cubff_run_epochs_workspace_bytes(num_programs, n_epochs))
+    return set_error(CUBFF_EINVAL, "run_epochs: workspace too small (%zu < %zu)", workspace_bytes,
+                     cubff_run_epochs_workspace_bytes(num_programs, n_epochs));
+  if (n_epochs == 0) return CUBFF_OK;
+  if ((num_programs / 2) * uint64_t(n_epochs) >= (1ull << 32))
+    return set_error(CUBFF_EINVAL, "run_epochs: num_programs/2 * n_epochs must be < 2^32");
+  int dev = 0;
+  CUBFF_CUDA_TRY(cudaGetDevice(&dev));
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  const uint64_t n = num_programs, P = n / 2, s0 = splitmix64(params_seed);
+  RunWs w = run_ws(d_workspace, n, n_epochs);
+  CUBFF_CUDA_TRY(cudaMemsetAsync(w.readycnt, 0, size_t(n_epochs) * P * sizeof(uint32_t), st));
+  CUBFF_CUDA_TRY(cudaMemsetAsync(w.queue, 0, size_t(n_epochs) * P * sizeof(uint32_t), st));
+  CUBFF_CUDA_TRY(cudaMemsetAsync(w.counters, 0,
+                                 size_t(n_epochs) * kPipeCountSlots * 2 * sizeof(unsigned long long), st));
+  CUBFF_CUDA_TRY(cudaMemsetAsync(w.ctl, 0, 4 * sizeof(uint32_t), st));
+  CUBFF_TRY(launch_mutation_masks(s0, first_epoch, n_epochs, n, mutation_prob, w.mutmask, st));
+  CUBFF_TRY(launch_inverse(d_shuf_idx, n_epochs, n, w.inv, st));
+  PipeArgs a;
+  a.soup = d_programs;
+  a.perm = d_shuf_idx;
+  a.n = n;
+  a.s0 = s0;
+  a.e0 = first_epoch;
+  a.n_epochs = n_epochs;
+  a.mutation_prob = mutation_prob;
+  a.d_num_indices = d_num_indices;
+  a.mutmask = w.mutmask;
+  a.inv = w.inv;
+  a.readycnt = w.readycnt;
+  a.queue = w.queue;
+  a.qctl = w.ctl;
+  a.error = reinterpret_cast<int *>(w.ctl + 2);
+  a.ops = w.counters;
+  a.lanes_per_pair64 = 0;
+  CUBFF_TRY(launch_pipeline(lang, a, dev, st));
+  reduce_counts_kernel<<<(n_epochs + 127) / 128, 128, 0, st>>>(w.counters, n_epochs, d_counts);
+  CUBFF_CUDA_TRY(cudaGetLastError());
+  return CUBFF_OK;
+}
+
+extern "C" int cubff_run_epochs_status(const void *d_workspace, uint64_t num_programs,
+                                       uint32_t n_epochs, void *stream) {
+  using namespace cubff;
+  if (!d_workspace) return set_error(CUBFF_EINVAL, "run_epochs_status: null workspace");
+  RunWs w = run_ws(const_cast<void *>(d_workspace), num_programs, n_epochs);
+  int err = 0;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  CUBFF_CUDA_TRY(cudaMemcpyAsync(&err, w.ctl + 2, sizeof(int), cudaMemcpyDeviceToHost, st));
+  CUBFF_CUDA_TRY(cudaStreamSynchronize(st));
+  if (err) return set_error(CUBFF_ETIMEDOUT, "run_epochs: a pipelined wait timed out");
+  return CUBFF_OK;
+}

@@ -102,6 +102,28 @@ int cubff_shuffle_indices(uint64_t params_seed, uint64_t first_epoch,
                           uint32_t *d_out, void *d_scratch,
                           size_t scratch_bytes, void *stream);
 
+/* The pipelined equivalent of n_epochs consecutive MutateAndRunPrograms
+ * launches (common_language.h:490-493 inside the epoch loop :432), epochs
+ * first_epoch .. first_epoch + n_epochs - 1 of one soup, in one persistent
+ * launch: a pair starts as soon as the two pairs of the previous epoch that
+ * wrote its programs are done.  d_shuf_idx holds the n_epochs shuffles
+ * ([n_epochs][num_programs], e.g. from cubff_shuffle_indices, 8-byte
+ * aligned); d_num_indices ([n_epochs], nullable = num_programs/2 each) the
+ * evaluated pair counts.  d_counts[2e], d_counts[2e+1] accumulate epoch e's op
+ * count and raw interpreter iterations.  d_workspace (256-byte aligned) holds
+ * cubff_run_epochs_workspace_bytes(num_programs, n_epochs) bytes.
+ * Asynchronous; cubff_run_epochs_status synchronizes the stream and reports
+ * CUBFF_ETIMEDOUT if a bounded wait inside the launch gave up.  Results are
+ * identical to the per-epoch launches. */
+size_t cubff_run_epochs_workspace_bytes(uint64_t num_programs, uint32_t n_epochs);
+int cubff_run_epochs(int lang, uint8_t *d_programs, const uint32_t *d_shuf_idx,
+                     const uint64_t *d_num_indices, uint64_t params_seed,
+                     uint64_t first_epoch, uint32_t n_epochs, uint32_t mutation_prob,
+                     uint64_t num_programs, unsigned long long *d_counts,
+                     void *d_workspace, size_t workspace_bytes, void *stream);
+int cubff_run_epochs_status(const void *d_workspace, uint64_t num_programs,
+                            uint32_t n_epochs, void *stream);
+
 /* Allocation-free variant of cubff_shuffle_indices.  It has no counterpart
  * in the reference.  It serves callers that cannot allocate device memory
  * (an application that owns the GPU's allocator, or a path that cannot take

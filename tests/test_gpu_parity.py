@@ -181,3 +181,33 @@ def test_long_run_through_emergence(name):
     assert epochs == spec["epoch"]
     assert ops == spec["ops"]
     assert shas == spec["sha"]
+
+
+@pytest.mark.parametrize("lang", ["bff_noheads", "bff", "bff8", "forth", "forthtrivial_reset",
+                                  "subleq", "rsubleq4", "bff_selfmove"])
+def test_run_epochs_kernel_matches_oracle(lang):
+    """cubff_run_epochs (pipelined, caller-owned buffers) over 24 epochs from
+    a seeded soup equals the oracle epoch by epoch (ops) and at the end (soup)."""
+    L = abi.lib()
+    n, seed, first, E = 8192, 21, 5, 24
+    soup = O.init_programs(O.seed_of(seed, 0), n)
+    want = soup.copy()
+    want_ops = []
+    for e in range(first, first + E):
+        s = O.pairing_shuffle(seed, e, n)
+        ops, _ = O.mutate_and_run(lang, want, s, O.seed_of(seed, e), 1 << 20, n // 2)
+        want_ops.append(ops)
+    d_soup = _dev(soup)
+    perm = torch.empty(E * n, dtype=torch.int32, device="cuda")
+    scratch = torch.empty(L.cubff_shuffle_scratch_bytes(n, E), dtype=torch.uint8, device="cuda")
+    abi.check(L.cubff_shuffle_indices(seed, first, E, n, perm.data_ptr(), scratch.data_ptr(),
+                                      scratch.numel(), None))
+    ws = torch.empty(L.cubff_run_epochs_workspace_bytes(n, E), dtype=torch.uint8, device="cuda")
+    counts = torch.zeros(2 * E, dtype=torch.int64, device="cuda")
+    abi.check(L.cubff_run_epochs(abi.language_id(lang), d_soup.data_ptr(), perm.data_ptr(), None,
+                                 seed, first, E, 1 << 20, n, counts.data_ptr(), ws.data_ptr(),
+                                 ws.numel(), None))
+    abi.check(L.cubff_run_epochs_status(ws.data_ptr(), n, E, None))
+    got_ops = _host(counts).reshape(E, 2)[:, 0].tolist()
+    assert got_ops == want_ops
+    assert np.array_equal(_host(d_soup), want)
