@@ -56,6 +56,8 @@ SIGNATURES = {
     "cubff_soup_run": (ci, [vp, u64, vp, vp, vp, vp]),
     "cubff_soup_selfrep": (ci, [vp, u64, vp]),
     "cubff_batch_run": (ci, [vp, vp, ci, u64, vp]),
+    "cubff_eval_pair": (ci, [ci, vp, vp, vp]),
+    "cubff_eval_selfrep": (ci, [ci, vp, u64, vp]),
 }
 
 _lib = None
@@ -157,10 +159,10 @@ class Soup:
         ops = np.zeros(n_epochs, dtype=np.uint64)
         raw = np.zeros(n_epochs, dtype=np.uint64)
         shuf = np.zeros(self.num_programs, dtype=np.uint32) if want_shuffle else None
-        ni = np.zeros(1, dtype=np.uint64)
+        ni = np.zeros(n_epochs, dtype=np.uint64)
         check(lib().cubff_soup_run(self.h, n_epochs, _p(ops), _p(raw), _p(shuf), _p(ni)))
         if want_shuffle:
-            return ops, raw, shuf, int(ni[0])
+            return ops, raw, shuf, ni
         return ops, raw
 
     def selfrep(self, epoch: int) -> np.ndarray:

@@ -29,9 +29,9 @@ BUILD = os.path.join(PKG, "_build", platform.machine())
 LIB = os.path.join(PKG, "libcubff_gb300.so")
 
 CUDA_SOURCES = ["epoch.cu", "pairing.cu", "pipeline.cu", "engine.cu", "batch.cu"]
-HOST_LIB_SOURCES: list = []
-PY_SOURCES: list = []
-CLI_SOURCES: list = []
+HOST_SOURCES = ["host/lang_host.cc", "host/simulation.cc"]  # C++ simulation API
+PY_SOURCES = ["host/cubff_py.cc"]                            # the `cubff` module
+CLI_SOURCES = ["host/main.cc"]                               # cubff_main
 
 GENCODE = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
@@ -62,7 +62,8 @@ def _newer(target, deps):
 
 def _deps():
     hdrs = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".h", ".cuh"))]
-    return hdrs + [os.path.join(REPO, "include", "cubff_gb300.h")]
+    inc = os.path.join(REPO, "include")
+    return hdrs + [os.path.join(inc, f) for f in os.listdir(inc) if f.endswith(".h")]
 
 
 def torch_pybind_include() -> str:
@@ -100,7 +101,7 @@ def build(verbose: bool = False, jobs: int = 0) -> str:
 
     def cxx_obj(src, extra=()):
         s = os.path.join(CSRC, src)
-        o = os.path.join(BUILD, src + ".o")
+        o = os.path.join(BUILD, src.replace("/", "_") + ".o")
         if not _newer(o, [s] + deps):
             return _run(["g++", "-c", s, "-o", o] + cxx_flags + list(extra))
         return ""
@@ -108,30 +109,29 @@ def build(verbose: bool = False, jobs: int = 0) -> str:
     py_inc = ["-I", sysconfig.get_paths()["include"], "-I", torch_pybind_include()]
     with cf.ThreadPoolExecutor(jobs) as ex:
         futs = [ex.submit(nv_obj, s) for s in CUDA_SOURCES]
-        futs += [ex.submit(cxx_obj, s) for s in HOST_LIB_SOURCES]
-        futs += [ex.submit(cxx_obj, s, py_inc) for s in PY_SOURCES]
+        futs += [ex.submit(cxx_obj, s) for s in HOST_SOURCES]
+        futs += [ex.submit(cxx_obj, s, py_inc + ["-fvisibility=hidden"]) for s in PY_SOURCES]
         futs += [ex.submit(cxx_obj, s) for s in CLI_SOURCES]
         logs = [f.result() for f in futs]
     if verbose:
         print("".join(logs))
 
-    lib_objs = [os.path.join(BUILD, s + ".o") for s in CUDA_SOURCES + HOST_LIB_SOURCES]
+    lib_objs = [os.path.join(BUILD, s + ".o") for s in CUDA_SOURCES]
+    host_objs = [os.path.join(BUILD, s.replace("/", "_") + ".o") for s in HOST_SOURCES]
     if not _newer(LIB, lib_objs):
         _run([nvcc, "-shared", "-o", LIB] + lib_objs + GENCODE +
              ["-Xlinker", "-soname,libcubff_gb300.so", "-ldl", "-lpthread"])
-    if not PY_SOURCES:
-        return LIB
     ext = sysconfig.get_config_var("EXT_SUFFIX")
     pymod = os.path.join(PKG, "cubff" + ext)
-    py_objs = [os.path.join(BUILD, s + ".o") for s in PY_SOURCES]
-    if not _newer(pymod, py_objs + [LIB]):
-        _run(["g++", "-shared", "-o", pymod] + py_objs +
-             ["-L", PKG, "-l:libcubff_gb300.so", "-Wl,-rpath,$ORIGIN"])
+    py_objs = [os.path.join(BUILD, s.replace("/", "_") + ".o") for s in PY_SOURCES]
+    if not _newer(pymod, py_objs + host_objs + [LIB]):
+        _run(["g++", "-shared", "-o", pymod] + py_objs + host_objs +
+             ["-L", PKG, "-l:libcubff_gb300.so", "-ldl", "-Wl,-rpath,$ORIGIN"])
     cli = os.path.join(PKG, "cubff_main")
-    cli_objs = [os.path.join(BUILD, s + ".o") for s in CLI_SOURCES]
-    if not _newer(cli, cli_objs + [LIB]):
-        _run(["g++", "-o", cli] + cli_objs +
-             ["-L", PKG, "-l:libcubff_gb300.so", "-Wl,-rpath,$ORIGIN"])
+    cli_objs = [os.path.join(BUILD, s.replace("/", "_") + ".o") for s in CLI_SOURCES]
+    if not _newer(cli, cli_objs + host_objs + [LIB]):
+        _run(["g++", "-o", cli] + cli_objs + host_objs +
+             ["-L", PKG, "-l:libcubff_gb300.so", "-ldl", "-Wl,-rpath,$ORIGIN"])
     return LIB
 
 

@@ -212,7 +212,7 @@ int cubff_soup::apply_reset() {
 }
 
 int cubff_soup::run(uint64_t n_epochs, uint64_t *ops_out, uint64_t *raw_out, uint32_t *last_shuffle,
-                    uint64_t *last_num_indices) {
+                    uint64_t *ni_out) {
   CUBFF_TRY(ensure_buffers());
   cudaStream_t st = eng->stream;
   const uint64_t n = p.num_programs;
@@ -262,6 +262,13 @@ int cubff_soup::run(uint64_t n_epochs, uint64_t *ops_out, uint64_t *raw_out, uin
       a.ops = d_counters + size_t(2) * kPipeCountSlots * c;
       a.lanes_per_pair64 = eng->lanes_per_pair64;
       CUBFF_TRY(launch_pipeline(p.lang, a, eng->device, st));
+      if (ni_out) {
+        if (p.pairing == CUBFF_PAIR_PATTERN)
+          CUBFF_CUDA_TRY(cudaMemcpyAsync(ni_out + done + c, d_num_indices + slot,
+                                         seg * sizeof(uint64_t), cudaMemcpyDeviceToHost, st));
+        else
+          for (uint64_t q = 0; q < seg; q++) ni_out[done + c + q] = n / 2;
+      }
       const uint64_t last = e + seg - 1;
       if (p.reset_interval && last % p.reset_interval == 0) {
         if (done + c + seg == n_epochs) pending_reset = true;
@@ -291,18 +298,10 @@ int cubff_soup::run(uint64_t n_epochs, uint64_t *ops_out, uint64_t *raw_out, uin
   }
   const uint64_t last = epoch + n_epochs - 1;
   epoch += n_epochs;
-  if (n_epochs > 0 && (last_shuffle || last_num_indices)) {
+  if (n_epochs > 0 && last_shuffle) {
     const uint64_t slot = last - perm_first;
-    if (last_shuffle)
-      CUBFF_CUDA_TRY(cudaMemcpyAsync(last_shuffle, d_perm + slot * n, n * sizeof(uint32_t),
-                                     cudaMemcpyDeviceToHost, st));
-    if (last_num_indices) {
-      if (p.pairing == CUBFF_PAIR_PATTERN)
-        CUBFF_CUDA_TRY(cudaMemcpyAsync(last_num_indices, d_num_indices + slot, sizeof(uint64_t),
-                                       cudaMemcpyDeviceToHost, st));
-      else
-        *last_num_indices = n / 2;
-    }
+    CUBFF_CUDA_TRY(cudaMemcpyAsync(last_shuffle, d_perm + slot * n, n * sizeof(uint32_t),
+                                   cudaMemcpyDeviceToHost, st));
     CUBFF_CUDA_TRY(cudaStreamSynchronize(st));
   }
   return CUBFF_OK;
@@ -526,17 +525,19 @@ int cubff_soup_set_epoch(cubff_soup *soup, uint64_t epoch, uint64_t reset_index)
 int cubff_soup_get_epoch(const cubff_soup *soup, uint64_t *epoch, uint64_t *reset_index) {
   if (!soup) return set_error(CUBFF_EINVAL, "get_epoch: null soup");
   if (epoch) *epoch = soup->epoch;
-  if (reset_index) *reset_index = soup->reset_index + (soup->pending_reset ? 1 : 0);
+  // The index the next reset uses (a reset still pending from the last run
+  // has not consumed it yet), as RunSimulation's reset_index at a callback.
+  if (reset_index) *reset_index = soup->reset_index;
   return CUBFF_OK;
 }
 
 int cubff_soup_run(cubff_soup *soup, uint64_t n_epochs, uint64_t *ops_per_epoch,
-                   uint64_t *raw_per_epoch, uint32_t *last_shuffle, uint64_t *last_num_indices) {
+                   uint64_t *raw_per_epoch, uint32_t *last_shuffle, uint64_t *num_indices_per_epoch) {
   if (!soup) return set_error(CUBFF_EINVAL, "soup_run: null soup");
   if (soup->p.pairing == CUBFF_PAIR_PATTERN && soup->pat_offs.empty())
     return set_error(CUBFF_EINVAL, "soup_run: pattern pairing needs cubff_soup_set_pattern");
   CUBFF_CUDA_TRY(cudaSetDevice(soup->eng->device));
-  return soup->run(n_epochs, ops_per_epoch, raw_per_epoch, last_shuffle, last_num_indices);
+  return soup->run(n_epochs, ops_per_epoch, raw_per_epoch, last_shuffle, num_indices_per_epoch);
 }
 
 int cubff_soup_selfrep(cubff_soup *soup, uint64_t epoch, uint64_t *result) {
@@ -557,6 +558,60 @@ int cubff_soup_selfrep(cubff_soup *soup, uint64_t epoch, uint64_t *result) {
   if (err == cudaSuccess) err = cudaStreamSynchronize(soup->eng->stream);
   cudaFree(d_res);
   if (err != cudaSuccess) return set_error(CUBFF_EDEVICE, "soup_selfrep: %s", cudaGetErrorString(err));
+  return st;
+}
+
+int cubff_eval_pair(int lang, uint8_t *tape, uint64_t *ops, uint64_t *raw) {
+  if (lang < 0 || lang >= kNumLangs) return set_error(CUBFF_ENOTFOUND, "unknown language %d", lang);
+  if (!tape || !ops) return set_error(CUBFF_EINVAL, "eval_pair: null argument");
+  // Two programs, identity pairing, no mutation: exactly one evaluated pair.
+  uint8_t *d = nullptr;
+  CUBFF_CUDA_TRY(cudaMalloc(&d, kPair + 2 * sizeof(uint32_t) + 2 * sizeof(unsigned long long) + 16));
+  uint8_t *d_soup = d;
+  uint32_t *d_perm = reinterpret_cast<uint32_t *>(d + kPair);
+  unsigned long long *d_cnt = reinterpret_cast<unsigned long long *>(d + kPair + 16);
+  const uint32_t perm[2] = {0, 1};
+  unsigned long long cnt[2] = {0, 0};
+  cudaError_t err = cudaMemcpy(d_soup, tape, kPair, cudaMemcpyHostToDevice);
+  if (err == cudaSuccess) err = cudaMemcpy(d_perm, perm, sizeof(perm), cudaMemcpyHostToDevice);
+  if (err == cudaSuccess) err = cudaMemset(d_cnt, 0, sizeof(cnt));
+  int st = CUBFF_OK;
+  if (err == cudaSuccess) {
+    EpochArgs a;
+    a.soup = d_soup;
+    a.perm = d_perm;
+    a.n = 2;
+    a.num_indices = 1;
+    a.d_num_indices = nullptr;
+    a.epoch_key = 0;
+    a.mutation_prob = 0;
+    a.ops = d_cnt;
+    a.raw = d_cnt + 1;
+    st = launch_epoch(lang, a, nullptr);
+  }
+  if (err == cudaSuccess && st == CUBFF_OK) err = cudaMemcpy(tape, d_soup, kPair, cudaMemcpyDeviceToHost);
+  if (err == cudaSuccess && st == CUBFF_OK) err = cudaMemcpy(cnt, d_cnt, sizeof(cnt), cudaMemcpyDeviceToHost);
+  cudaFree(d);
+  if (err != cudaSuccess) return set_error(CUBFF_EDEVICE, "eval_pair: %s", cudaGetErrorString(err));
+  if (st != CUBFF_OK) return st;
+  *ops = cnt[0];
+  if (raw) *raw = cnt[1];
+  return CUBFF_OK;
+}
+
+int cubff_eval_selfrep(int lang, const uint8_t *program, uint64_t epoch_key, uint64_t *result) {
+  if (lang < 0 || lang >= kNumLangs) return set_error(CUBFF_ENOTFOUND, "unknown language %d", lang);
+  if (!program || !result) return set_error(CUBFF_EINVAL, "eval_selfrep: null argument");
+  uint8_t *d = nullptr;
+  CUBFF_CUDA_TRY(cudaMalloc(&d, kTape + sizeof(uint64_t)));
+  uint64_t *d_res = reinterpret_cast<uint64_t *>(d + kTape);
+  cudaError_t err = cudaMemcpy(d, program, kTape, cudaMemcpyHostToDevice);
+  int st = CUBFF_OK;
+  if (err == cudaSuccess) st = launch_selfrep(lang, d, epoch_key, 1, 1, d_res, nullptr);
+  if (err == cudaSuccess && st == CUBFF_OK)
+    err = cudaMemcpy(result, d_res, sizeof(uint64_t), cudaMemcpyDeviceToHost);
+  cudaFree(d);
+  if (err != cudaSuccess) return set_error(CUBFF_EDEVICE, "eval_selfrep: %s", cudaGetErrorString(err));
   return st;
 }
 

@@ -60,7 +60,7 @@ struct cubff_soup {
   int fill_pairing(uint64_t first, uint32_t count);
   int apply_reset();
   int run(uint64_t n_epochs, uint64_t *ops_out, uint64_t *raw_out, uint32_t *last_shuffle,
-          uint64_t *last_num_indices);
+          uint64_t *ni_out);
 };
 
 namespace cubff {

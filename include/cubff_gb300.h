@@ -176,8 +176,10 @@ int cubff_soup_write(cubff_soup *soup, const uint8_t *src, uint64_t offset,
 int cubff_soup_read(cubff_soup *soup, uint8_t *dst, uint64_t offset,
                     uint64_t nbytes);
 
-/* Epoch counter and reset index (restored from a checkpoint header,
- * common_language.h:354-360). */
+/* Epoch counter (the next epoch to run) and reset index (the index the
+ * next reset will use, i.e. the value RunSimulation holds at a callback and
+ * saves in checkpoints), restored from a checkpoint header
+ * (common_language.h:354-360). */
 int cubff_soup_set_epoch(cubff_soup *soup, uint64_t epoch, uint64_t reset_index);
 int cubff_soup_get_epoch(const cubff_soup *soup, uint64_t *epoch,
                          uint64_t *reset_index);
@@ -186,17 +188,30 @@ int cubff_soup_get_epoch(const cubff_soup *soup, uint64_t *epoch,
  * pairing, MutateAndRunPrograms and resets.  A reset due after the LAST epoch
  * of the call is applied at the start of the next call, so that the caller's
  * callback sees the soup as the reference's callback does (:582 before
- * :590).  ops_per_epoch / raw_per_epoch: host arrays of n_epochs entries
- * (raw nullable).  last_shuffle (nullable, num_programs entries) receives the
- * last epoch's shuffle_idx; last_num_indices (nullable) its pair count. */
+ * :590).  ops_per_epoch / raw_per_epoch / num_indices_per_epoch: host arrays
+ * of n_epochs entries (nullable): op count, raw interpreter iterations and
+ * evaluated pairs (num_indices) of each epoch.  last_shuffle (nullable,
+ * num_programs entries) receives the last epoch's shuffle_idx. */
 int cubff_soup_run(cubff_soup *soup, uint64_t n_epochs,
                    uint64_t *ops_per_epoch, uint64_t *raw_per_epoch,
-                   uint32_t *last_shuffle, uint64_t *last_num_indices);
+                   uint32_t *last_shuffle, uint64_t *num_indices_per_epoch);
 
 /* Self-replication scores of the soup's programs (CheckSelfRep with
  * seed(epoch)); result has num_programs entries; programs past
  * (num_programs/32)*32, which the reference's launch does not cover, get 0. */
 int cubff_soup_selfrep(cubff_soup *soup, uint64_t epoch, uint64_t *result);
+
+/* One pair tape (128 host bytes, modified in place) evaluated on the device
+ * with the 8192-step limit and no mutation: Language::Evaluate as used by
+ * RunSingleParsedProgram (common_language.h:280-296).  *ops gets the
+ * reference-counted ops, *raw (nullable) the interpreter iterations. */
+int cubff_eval_pair(int lang, uint8_t *tape, uint64_t *ops, uint64_t *raw);
+
+/* EvalParsedSelfrep (common_language.h:326-342): the self-replication score
+ * of one 64-byte host program with epoch_key = SplitMix64(SplitMix64(seed) ^
+ * SplitMix64(epoch)). */
+int cubff_eval_selfrep(int lang, const uint8_t *program, uint64_t epoch_key,
+                       uint64_t *result);
 
 /* ---- layer 3: batching ------------------------------------------------- */
 /* Advances every soup by n_epochs epochs; each epoch of all soups is one
