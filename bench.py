@@ -58,6 +58,8 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batch", action="store_true")
+    ap.add_argument("--no-serving", action="store_true")
+    ap.add_argument("--serving-jobs", type=int, default=200)
     return ap.parse_args()
 
 
@@ -220,9 +222,10 @@ def gpu_e2e(torch, abi, steps: int):
 
 
 def batch_compare(torch, abi, epochs: int):
-    """The 64-soup mix (seeds 100..163): one launch per epoch for all soups
-    (cubff_batch_run) against one soup at a time (cubff_soup_run), same GPU,
-    same epochs; op counts must agree."""
+    """The 64-soup mix (seeds 100..163): all soups in shared pipelined
+    launches, one launch group per language on its own stream
+    (cubff_batch_run), against one soup at a time (cubff_soup_run), same GPU,
+    same epochs; op counts and soup bytes must agree."""
     import numpy as np
     from cubff_gb300.workloads import batch_mix
     specs = batch_mix(epochs)
@@ -262,6 +265,38 @@ def batch_compare(torch, abi, epochs: int):
             "programs_total": int(sum(s.num_programs for s in specs)),
             "per_soup_steps_per_s": total_ops / t_seq, "batched_steps_per_s": total_ops / t_bat,
             "batched_over_per_soup": t_seq / t_bat, "bit_identical": bool(same)}
+
+
+def serving_sample(torch, abi, jobs: int, verify: int = 4):
+    """The serving stream (Poisson arrivals at 20 jobs/s; job j: seed j, size
+    log-uniform in [2^10, 2^17], 64..4096 epochs, language and mutation rate
+    as in the batched mix): the first `jobs` jobs replayed in real time
+    against a server with a 64 GiB device-memory budget.  A seeded sample of
+    `verify` jobs is re-run alone (cubff_soup_run) and must match."""
+    import numpy as np
+    from cubff_gb300 import serving
+    from cubff_gb300.workloads import serving_jobs
+    arrivals, specs = serving_jobs(jobs)
+    rng = np.random.default_rng(11)
+    small = [i for i in range(jobs)
+             if specs[i].num_programs * specs[i].epochs <= (1 << 14) * 1024]
+    check = set(rng.choice(small, size=min(verify, len(small)), replace=False).tolist())
+    eng = abi.Engine(0)
+    rep = serving.replay(eng, arrivals, specs, 64 << 30, keep=check)
+    same = True
+    for i in sorted(check):
+        s = specs[i]
+        soup = abi.Soup(eng, s.lang, s.num_programs, s.seed, s.mutation_prob)
+        ops = soup.run(s.epochs)[0]
+        got_soup, got_ops = rep["results"][i]
+        same &= bool(np.array_equal(ops, got_ops) and np.array_equal(soup.read(), got_soup))
+        soup.close()
+    eng.close()
+    out = serving.summary(rep)
+    out.update({"rate_per_s": 20.0, "sample": f"jobs 0..{jobs - 1} of the 2000-job stream",
+                "hbm_budget_gib": 64, "verified_alone": sorted(int(i) for i in check),
+                "same_alone_and_in_mix": same})
+    return out
 
 
 def cpu_sample(budget_s: float = 15.0, max_epochs: int = 10**9):
@@ -390,6 +425,8 @@ def main():
                     "wall_s": e2["total_s"]}}
     if not args.no_batch:
         line["batched"] = batch_compare(torch, abi, 64)
+    if not args.no_serving:
+        line["serving"] = serving_sample(torch, abi, args.serving_jobs)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_sample()
     if rank == 0:

@@ -28,6 +28,12 @@ class SoupParams(ctypes.Structure):
                 ("pairing", ci), ("reset_interval", u64), ("zero_init", ci)]
 
 
+class JobInfo(ctypes.Structure):
+    _fields_ = [("job_id", u64), ("status", ci), ("num_programs", u64), ("n_epochs", u64),
+                ("total_ops", u64), ("submit_s", ctypes.c_double), ("start_s", ctypes.c_double),
+                ("finish_s", ctypes.c_double)]
+
+
 # name -> (restype, argtypes)
 SIGNATURES = {
     "cubff_status_string": (cp, [ci]),
@@ -56,6 +62,14 @@ SIGNATURES = {
     "cubff_soup_run": (ci, [vp, u64, vp, vp, vp, vp]),
     "cubff_soup_selfrep": (ci, [vp, u64, vp]),
     "cubff_batch_run": (ci, [vp, vp, ci, u64, vp]),
+    "cubff_soup_footprint_bytes": (u64, [ctypes.POINTER(SoupParams)]),
+    "cubff_server_create": (ci, [vp, u64, u32, ctypes.POINTER(vp)]),
+    "cubff_server_destroy": (ci, [vp]),
+    "cubff_server_submit": (ci, [vp, ctypes.POINTER(SoupParams), u64, ctypes.POINTER(u64)]),
+    "cubff_server_poll": (ci, [vp, ctypes.POINTER(JobInfo), ci, ctypes.POINTER(ci),
+                               ctypes.c_double]),
+    "cubff_server_fetch": (ci, [vp, u64, vp, vp]),
+    "cubff_server_stats": (ci, [vp, vp, vp, vp, vp]),
     "cubff_eval_pair": (ci, [ci, vp, vp, vp]),
     "cubff_eval_selfrep": (ci, [ci, vp, u64, vp]),
 }
@@ -187,3 +201,60 @@ def batch_run(engine: Engine, soups, n_epochs: int) -> np.ndarray:
     ops = np.zeros((len(soups), n_epochs), dtype=np.uint64)
     check(lib().cubff_batch_run(engine.h, arr, len(soups), n_epochs, _p(ops)))
     return ops
+
+
+def soup_params(lang: str, num_programs: int, seed: int = 0, mutation_prob: int = 1 << 18,
+                pairing: int = PAIR_SHUFFLE, reset_interval: int = 0,
+                zero_init: bool = False) -> SoupParams:
+    return SoupParams(language_id(lang), num_programs, seed, mutation_prob, pairing,
+                      reset_interval, int(zero_init))
+
+
+def footprint_bytes(params: SoupParams) -> int:
+    return int(lib().cubff_soup_footprint_bytes(ctypes.byref(params)))
+
+
+class Server:
+    """A job server on an engine (cubff_server_*).  The server's worker owns
+    the engine while the server exists."""
+
+    def __init__(self, engine: Engine, hbm_budget_bytes: int, round_epochs: int = 0):
+        self.engine = engine
+        h = vp()
+        check(lib().cubff_server_create(engine.h, hbm_budget_bytes, round_epochs, ctypes.byref(h)))
+        self.h = h
+
+    def submit(self, params: SoupParams, n_epochs: int) -> int:
+        jid = u64(0)
+        check(lib().cubff_server_submit(self.h, ctypes.byref(params), n_epochs, ctypes.byref(jid)))
+        return int(jid.value)
+
+    def poll(self, max_jobs: int = 64, wait_s: float = 0.0):
+        """Finished jobs since the last poll: a list of dicts (JobInfo fields)."""
+        buf = (JobInfo * max_jobs)()
+        n = ci(0)
+        check(lib().cubff_server_poll(self.h, buf, max_jobs, ctypes.byref(n), wait_s))
+        return [{f: getattr(buf[i], f) for f, _ in JobInfo._fields_} for i in range(n.value)]
+
+    def fetch(self, job_id: int, num_programs: int, n_epochs: int):
+        """(soup bytes, per-epoch op counts) of a finished job."""
+        soup = np.zeros(num_programs * 64, dtype=np.uint8)
+        ops = np.zeros(n_epochs, dtype=np.uint64)
+        check(lib().cubff_server_fetch(self.h, job_id, _p(soup), _p(ops)))
+        return soup, ops
+
+    def stats(self):
+        v = [u64(0) for _ in range(4)]
+        check(lib().cubff_server_stats(self.h, *[ctypes.byref(x) for x in v]))
+        return dict(zip(["queued", "running", "finished", "hbm_bytes"], [int(x.value) for x in v]))
+
+    def close(self):
+        if self.h:
+            lib().cubff_server_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

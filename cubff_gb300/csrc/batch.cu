@@ -1,101 +1,330 @@
-// batch.cu — many independent soups (uneven size, language, mutation rate)
-// advanced together: one persistent launch per epoch covers every pair of
-// every soup.  A descriptor per soup (EpochArgs + language + first virtual
-// CTA) lets each CTA find its soup by binary search over the CTA prefix; the
-// language switch is uniform per CTA, so there is no divergence from mixing
-// languages.
+// batch.cu — pipelined runs of one or more soups (cubff_soup_run,
+// cubff_batch_run).
+//
+// The soups of a run (any languages, sizes, mutation rates and pairing
+// modes) are split into launch groups: one language, at most kMaxPipeSoups
+// soups each.  A group advances in rounds; a round is one persistent
+// pipeline launch (pipeline.cu) covering the next segment of epochs of every
+// soup in the group.  A soup's segment ends where its cached pairings end,
+// at a reset epoch (a reset rewrites every program at once,
+// common_language.h:590-595), at the end of its op-counter chunk, or at the
+// end of the run.  Groups run on streams of their own, forked from and joined
+// back to the engine stream, so the launches of different languages overlap;
+// the host enqueues all rounds without waiting, except to read the op
+// counters back every kCounterChunk epochs and for host-computed (pattern)
+// pairings.
 #include <algorithm>
+#include <memory>
+#include <numeric>
 #include <vector>
 
+#include "common.cuh"
 #include "engine_impl.h"
-#include "epoch_body.cuh"
+#include "internal.h"
 
 namespace cubff {
 
-struct BatchDesc {
-  EpochArgs a;
-  int lang;
-  uint32_t block_begin;  // first virtual CTA of this soup
-};
-
-namespace {
-
-__global__ void __launch_bounds__(kThreads)
-    batch_epoch_kernel(const BatchDesc *__restrict__ descs, int n_soups, uint32_t total_blocks) {
-  extern __shared__ __align__(16) uint8_t smem[];
-  for (uint32_t vb = blockIdx.x; vb < total_blocks; vb += gridDim.x) {
-    int lo = 0, hi = n_soups - 1;
-    while (lo < hi) {
-      const int mid = (lo + hi + 1) >> 1;
-      if (descs[mid].block_begin <= vb) lo = mid; else hi = mid - 1;
-    }
-    const EpochArgs a = descs[lo].a;
-    const uint64_t blk = vb - descs[lo].block_begin;
-    switch (descs[lo].lang) {
-      case kBff: epoch_cta<kBff>(a, blk, smem); break;
-      case kBffNoheads: epoch_cta<kBffNoheads>(a, blk, smem); break;
-      case kBffNoheads4bit: epoch_cta<kBffNoheads4bit>(a, blk, smem); break;
-      case kBffPerm: epoch_cta<kBffPerm>(a, blk, smem); break;
-      case kBff8: epoch_cta<kBff8>(a, blk, smem); break;
-      case kBff8Noheads: epoch_cta<kBff8Noheads>(a, blk, smem); break;
-      case kBffSelfmove: epoch_cta<kBffSelfmove>(a, blk, smem); break;
-      case kForth: epoch_cta<kForth>(a, blk, smem); break;
-      case kForthcopy: epoch_cta<kForthcopy>(a, blk, smem); break;
-      case kForthtrivial: epoch_cta<kForthtrivial>(a, blk, smem); break;
-      case kForthtrivialReset: epoch_cta<kForthtrivialReset>(a, blk, smem); break;
-      case kSubleq: epoch_cta<kSubleq>(a, blk, smem); break;
-      default: epoch_cta<kRsubleq4>(a, blk, smem); break;
-    }
-    __syncthreads();  // shared memory is reused by the next virtual CTA
-  }
-}
-
-}  // namespace
-
-int launch_batch_epoch(const BatchDesc *d_descs, int n_soups, uint32_t total_blocks,
-                       int device, cudaStream_t stream) {
-  static int max_grid[64] = {0};
-  int &g = max_grid[device & 63];
-  if (g == 0) {
-    CUBFF_CUDA_TRY(cudaFuncSetAttribute(batch_epoch_kernel,
-                                        cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                        static_cast<int>(kMaxEpochSmem)));
-    int per_sm = 0, sms = 0;
-    CUBFF_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batch_epoch_kernel,
-                                                                 kThreads, kMaxEpochSmem));
-    CUBFF_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
-    g = std::max(1, per_sm) * sms;
-  }
-  const uint32_t grid = std::min<uint32_t>(total_blocks, static_cast<uint32_t>(g));
-  batch_epoch_kernel<<<grid, kThreads, kMaxEpochSmem, stream>>>(d_descs, n_soups, total_blocks);
-  CUBFF_CUDA_TRY(cudaGetLastError());
-  return CUBFF_OK;
-}
+// Keeps queue ids (task + 1, uint32) and the queue heads, which overshoot the
+// task count by at most 32 per warp, clear of 2^32.
+static constexpr uint64_t kMaxTasksPerLaunch = (1ull << 31) - (1ull << 22);
 
 }  // namespace cubff
 
 using namespace cubff;
 
-int cubff_engine::reserve_batch(size_t n_desc) {
-  if (n_desc <= desc_cap) return CUBFF_OK;
-  release_batch();
-  CUBFF_CUDA_TRY(cudaMalloc(&d_desc, n_desc * sizeof(BatchDesc)));
-  CUBFF_CUDA_TRY(cudaMallocHost(&h_desc, n_desc * sizeof(BatchDesc)));
-  CUBFF_CUDA_TRY(cudaMalloc(&d_bcnt, n_desc * 2 * sizeof(unsigned long long)));
-  CUBFF_CUDA_TRY(cudaMallocHost(&h_bcnt, n_desc * 2 * sizeof(unsigned long long)));
-  desc_cap = n_desc;
+int cubff_engine::reserve_pipe(size_t groups, size_t entries) {
+  while (streams.size() < groups) {
+    cudaStream_t s = nullptr;
+    CUBFF_CUDA_TRY(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+    streams.push_back(s);
+  }
+  while (events.size() < groups + 1) {
+    cudaEvent_t e = nullptr;
+    CUBFF_CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    events.push_back(e);
+  }
+  if (groups > ctl_groups) {
+    if (d_ctl) cudaFree(d_ctl);
+    if (h_ctl) cudaFreeHost(h_ctl);
+    d_ctl = h_ctl = nullptr;
+    ctl_groups = 0;
+    CUBFF_CUDA_TRY(cudaMalloc(&d_ctl, groups * 4 * sizeof(uint32_t)));
+    CUBFF_CUDA_TRY(cudaMallocHost(&h_ctl, groups * 4 * sizeof(uint32_t)));
+    ctl_groups = groups;
+  }
+  if (entries > queue_cap) {
+    if (d_queue) cudaFree(d_queue);
+    d_queue = nullptr;
+    queue_cap = 0;
+    CUBFF_CUDA_TRY(cudaMalloc(&d_queue, entries * sizeof(uint32_t)));
+    CUBFF_CUDA_TRY(cudaMemset(d_queue, 0, entries * sizeof(uint32_t)));
+    queue_cap = entries;
+  }
   return CUBFF_OK;
 }
 
-void cubff_engine::release_batch() {
-  if (d_desc) cudaFree(d_desc);
-  if (h_desc) cudaFreeHost(h_desc);
-  if (d_bcnt) cudaFree(d_bcnt);
-  if (h_bcnt) cudaFreeHost(h_bcnt);
-  d_desc = h_desc = nullptr;
-  d_bcnt = h_bcnt = nullptr;
-  desc_cap = 0;
+void cubff_engine::release_pipe() {
+  for (cudaStream_t s : streams) cudaStreamDestroy(s);
+  for (cudaEvent_t e : events) cudaEventDestroy(e);
+  streams.clear();
+  events.clear();
+  if (d_queue) cudaFree(d_queue);
+  if (d_ctl) cudaFree(d_ctl);
+  if (h_ctl) cudaFreeHost(h_ctl);
+  d_queue = nullptr;
+  d_ctl = h_ctl = nullptr;
+  queue_cap = ctl_groups = 0;
 }
+
+namespace cubff {
+namespace {
+
+struct Group {
+  int lang;
+  std::vector<int> members;  // indices into the run's soups
+  cudaStream_t st;
+  size_t qoff;               // first entry of the group's ready queue in d_queue
+};
+
+// Per-soup progress of a run.
+struct Progress {
+  uint64_t done = 0;   // epochs of this run enqueued
+  uint64_t cbase = 0;  // run epoch of counter row 0
+  uint32_t seg = 0;    // epochs of the round being built
+};
+
+}  // namespace
+
+// Reads back and reduces the op counters of every soup of the run, and the
+// groups' error flags.  The groups' streams must be idle (synchronised).
+static int read_counters(cubff_soup *const *soups, const std::vector<Group> &groups,
+                         std::vector<Progress> &pr, uint64_t *const *ops, uint64_t *const *raw,
+                         const uint32_t *h_ctl, bool *timed_out) {
+  for (const Group &g : groups) {
+    if (h_ctl[4 * (&g - groups.data()) + 2] != 0) *timed_out = true;
+    for (int i : g.members) {
+      const uint64_t rows = pr[i].done - pr[i].cbase;
+      const unsigned long long *h = soups[i]->h_counters;
+      for (uint64_t q = 0; q < rows; q++) {
+        uint64_t o = 0, r = 0;
+        for (int sl = 0; sl < kPipeCountSlots; sl++) {
+          o += h[(q * kPipeCountSlots + sl) * 2];
+          r += h[(q * kPipeCountSlots + sl) * 2 + 1];
+        }
+        if (ops && ops[i]) ops[i][pr[i].cbase + q] = o;
+        if (raw && raw[i]) raw[i][pr[i].cbase + q] = r;
+      }
+    }
+  }
+  return CUBFF_OK;
+}
+
+// Enqueues the copies that read_counters consumes, on each group's stream.
+static int copy_counters(cubff_soup *const *soups, const std::vector<Group> &groups,
+                         const std::vector<Progress> &pr, const cubff_engine *eng) {
+  for (size_t gi = 0; gi < groups.size(); gi++) {
+    const Group &g = groups[gi];
+    for (int i : g.members) {
+      const uint64_t rows = pr[i].done - pr[i].cbase;
+      if (rows)
+        CUBFF_CUDA_TRY(cudaMemcpyAsync(soups[i]->h_counters, soups[i]->d_counters,
+                                       rows * kPipeCountSlots * 2 * sizeof(unsigned long long),
+                                       cudaMemcpyDeviceToHost, g.st));
+    }
+    CUBFF_CUDA_TRY(cudaMemcpyAsync(eng->h_ctl + 4 * gi, eng->d_ctl + 4 * gi, 4 * sizeof(uint32_t),
+                                   cudaMemcpyDeviceToHost, g.st));
+  }
+  return CUBFF_OK;
+}
+
+int run_soups(cubff_engine *eng, cubff_soup *const *soups, int n_soups, uint64_t n_epochs,
+              uint64_t *const *ops, uint64_t *const *raw, uint64_t *const *ni) {
+  if (n_epochs == 0 || n_soups == 0) return CUBFF_OK;
+  constexpr uint64_t kChunk = cubff_soup::kCounterChunk;
+  for (int i = 0; i < n_soups; i++) CUBFF_TRY(soups[i]->ensure_buffers());
+
+  // Launch groups: by language, at most kMaxPipeSoups soups each.
+  std::vector<int> order(n_soups);
+  std::iota(order.begin(), order.end(), 0);
+  std::stable_sort(order.begin(), order.end(),
+                   [&](int a, int b) { return soups[a]->p.lang < soups[b]->p.lang; });
+  std::vector<Group> groups;
+  size_t entries = 0;
+  for (int i : order) {
+    if (groups.empty() || groups.back().lang != soups[i]->p.lang ||
+        groups.back().members.size() == size_t(kMaxPipeSoups))
+      groups.push_back(Group{soups[i]->p.lang, {}, nullptr, entries});
+    groups.back().members.push_back(i);
+    entries += size_t(soups[i]->batch) * (soups[i]->p.num_programs / 2);
+  }
+  const size_t G = groups.size();
+  CUBFF_TRY(eng->reserve_pipe(G, entries));
+  cudaStream_t main = eng->stream;
+  for (size_t g = 0; g < G; g++) groups[g].st = G == 1 ? main : eng->streams[g];
+
+  // State left behind by a launch that gave up.
+  if (eng->dirty) {
+    CUBFF_CUDA_TRY(cudaMemsetAsync(eng->d_queue, 0, eng->queue_cap * sizeof(uint32_t), main));
+    eng->dirty = false;
+  }
+  for (int i = 0; i < n_soups; i++) {
+    cubff_soup *s = soups[i];
+    if (s->dirty) {
+      CUBFF_CUDA_TRY(cudaMemsetAsync(s->d_readycnt, 0,
+                                     size_t(s->batch) * (s->p.num_programs / 2) * sizeof(uint32_t),
+                                     main));
+      s->dirty = false;
+    }
+  }
+  CUBFF_CUDA_TRY(cudaMemsetAsync(eng->d_ctl, 0, G * 4 * sizeof(uint32_t), main));
+  if (G > 1) {
+    CUBFF_CUDA_TRY(cudaEventRecord(eng->events[0], main));
+    for (size_t g = 0; g < G; g++) CUBFF_CUDA_TRY(cudaStreamWaitEvent(groups[g].st, eng->events[0], 0));
+  }
+
+  std::vector<Progress> pr(n_soups);
+  const uint64_t first_rows = std::min<uint64_t>(n_epochs, kChunk);
+  for (const Group &g : groups) {
+    for (int i : g.members) {
+      cubff_soup *s = soups[i];
+      if (s->pending_reset) {
+        CUBFF_TRY(s->apply_reset(g.st));
+        s->pending_reset = false;
+      }
+      CUBFF_CUDA_TRY(cudaMemsetAsync(s->d_counters, 0,
+                                     first_rows * kPipeCountSlots * 2 * sizeof(unsigned long long),
+                                     g.st));
+    }
+  }
+
+  std::unique_ptr<PipeBatch> b(new PipeBatch);
+  bool timed_out = false;
+  while (true) {
+    // A soup whose counter chunk is full: read every soup's counters back.
+    bool flush = false;
+    for (int i = 0; i < n_soups; i++)
+      flush |= pr[i].done < n_epochs && pr[i].done - pr[i].cbase == kChunk;
+    if (flush) {
+      CUBFF_TRY(copy_counters(soups, groups, pr, eng));
+      for (const Group &g : groups) CUBFF_CUDA_TRY(cudaStreamSynchronize(g.st));
+      CUBFF_TRY(read_counters(soups, groups, pr, ops, raw, eng->h_ctl, &timed_out));
+      if (timed_out) break;
+      for (const Group &g : groups) {
+        for (int i : g.members) {
+          pr[i].cbase = pr[i].done;
+          const uint64_t rows = std::min<uint64_t>(n_epochs - pr[i].done, kChunk);
+          if (rows)
+            CUBFF_CUDA_TRY(cudaMemsetAsync(soups[i]->d_counters, 0,
+                                           rows * kPipeCountSlots * 2 * sizeof(unsigned long long),
+                                           g.st));
+        }
+      }
+    }
+
+    bool any = false;
+    for (size_t gi = 0; gi < G; gi++) {
+      Group &g = groups[gi];
+      PipeBatch &pb = *b;
+      pb.n_soups = 0;
+      uint64_t tasks = 0, pairs = 0;
+      uint32_t initial = 0;
+      for (int i : g.members) {
+        cubff_soup *s = soups[i];
+        Progress &p = pr[i];
+        p.seg = 0;
+        if (p.done >= n_epochs) continue;
+        const uint64_t n = s->p.num_programs, P = n / 2;
+        const uint64_t e = s->epoch + p.done;
+        if (s->perm_count == 0 || e < s->perm_first || e >= s->perm_first + s->perm_count)
+          CUBFF_TRY(s->fill_pairing(e, static_cast<uint32_t>(std::min<uint64_t>(s->batch, n_epochs - p.done)),
+                                    g.st));
+        uint64_t seg = std::min<uint64_t>(s->perm_first + s->perm_count - e, n_epochs - p.done);
+        seg = std::min<uint64_t>(seg, p.cbase + kChunk - p.done);
+        if (s->p.reset_interval) {
+          const uint64_t r = e + (s->p.reset_interval - e % s->p.reset_interval) % s->p.reset_interval;
+          seg = std::min<uint64_t>(seg, r - e + 1);
+        }
+        if (tasks + P * seg > kMaxTasksPerLaunch) {
+          if (pb.n_soups > 0) continue;  // runs in a later round
+          seg = std::max<uint64_t>(1, kMaxTasksPerLaunch / P);
+        }
+        const uint64_t slot = e - s->perm_first;
+        PipeSoup &d = pb.soups[pb.n_soups++];
+        d.soup = s->d_soup;
+        d.perm = s->d_perm + slot * n;
+        d.inv = s->d_inv + slot * n;
+        d.mutmask = s->d_mutmask + slot * P;
+        d.readycnt = s->d_readycnt;
+        d.num_indices = s->p.pairing == CUBFF_PAIR_PATTERN ? s->d_num_indices + slot : nullptr;
+        d.ops = s->d_counters + (p.done - p.cbase) * kPipeCountSlots * 2;
+        d.n = n;
+        d.s0 = s->s0;
+        d.e0 = e;
+        d.npairs = static_cast<uint32_t>(P);
+        d.mutation_prob = s->p.mutation_prob;
+        d.task_base = static_cast<uint32_t>(tasks);
+        d.init_base = initial;
+        d.lang = s->p.lang;
+        d.n_epochs = static_cast<uint32_t>(seg);
+        tasks += P * seg;
+        initial += static_cast<uint32_t>(P);
+        pairs += P;
+        p.seg = static_cast<uint32_t>(seg);
+        if (ni && ni[i]) {
+          for (uint64_t q = 0; q < seg; q++)
+            ni[i][p.done + q] = s->p.pairing == CUBFF_PAIR_PATTERN ? s->pat_ni[slot + q] : P;
+        }
+      }
+      if (pb.n_soups == 0) continue;
+      any = true;
+      PipeQueue &q = pb.queue;
+      q.queue = eng->d_queue + g.qoff;
+      q.ctl = eng->d_ctl + 4 * gi;
+      q.total = static_cast<uint32_t>(tasks);
+      q.initial = initial;
+      q.first_soup = 0;
+      q.n_soups = static_cast<uint32_t>(pb.n_soups);
+      q.lang = g.lang;
+      pb.error = reinterpret_cast<int *>(eng->d_ctl + 4 * gi + 2);
+      CUBFF_CUDA_TRY(cudaMemsetAsync(q.ctl, 0, 2 * sizeof(uint32_t), g.st));  // head, tail
+      CUBFF_TRY(launch_pipeline(pb, pairs, eng->lanes_per_pair64, eng->device, g.st));
+      for (int i : g.members) {
+        cubff_soup *s = soups[i];
+        Progress &p = pr[i];
+        if (p.seg == 0) continue;
+        const uint64_t last = s->epoch + p.done + p.seg - 1;
+        p.done += p.seg;
+        if (s->p.reset_interval && last % s->p.reset_interval == 0) {
+          if (p.done == n_epochs) s->pending_reset = true;
+          else CUBFF_TRY(s->apply_reset(g.st));
+        }
+      }
+    }
+    if (!any) break;
+  }
+
+  if (!timed_out) {
+    CUBFF_TRY(copy_counters(soups, groups, pr, eng));
+    for (const Group &g : groups) CUBFF_CUDA_TRY(cudaStreamSynchronize(g.st));
+    CUBFF_TRY(read_counters(soups, groups, pr, ops, raw, eng->h_ctl, &timed_out));
+  }
+  if (G > 1) {
+    for (size_t g = 0; g < G; g++) {
+      CUBFF_CUDA_TRY(cudaEventRecord(eng->events[1 + g], groups[g].st));
+      CUBFF_CUDA_TRY(cudaStreamWaitEvent(main, eng->events[1 + g], 0));
+    }
+  }
+  for (int i = 0; i < n_soups; i++) soups[i]->epoch += pr[i].done;
+  if (timed_out) {
+    eng->dirty = true;
+    for (int i = 0; i < n_soups; i++) soups[i]->dirty = true;
+    return set_error(CUBFF_ETIMEDOUT,
+                     "a pipelined epoch wait timed out; the soups' state is invalid");
+  }
+  return CUBFF_OK;
+}
+
+}  // namespace cubff
 
 extern "C" int cubff_batch_run(cubff_engine *eng, cubff_soup **soups, int n_soups,
                                uint64_t n_epochs, uint64_t *ops) {
@@ -110,76 +339,7 @@ extern "C" int cubff_batch_run(cubff_engine *eng, cubff_soup **soups, int n_soup
       if (soups[t] == soups[s]) return set_error(CUBFF_EINVAL, "batch_run: soup %d repeated", s);
   }
   CUBFF_CUDA_TRY(cudaSetDevice(eng->device));
-  cudaStream_t st = eng->stream;
-  for (int s = 0; s < n_soups; s++) {
-    CUBFF_TRY(soups[s]->ensure_buffers());
-    if (soups[s]->pending_reset) {
-      CUBFF_TRY(soups[s]->apply_reset());
-      soups[s]->pending_reset = false;
-    }
-  }
-  std::vector<uint32_t> block_begin(n_soups);
-  uint64_t total = 0;
-  for (int s = 0; s < n_soups; s++) {
-    block_begin[s] = static_cast<uint32_t>(total);
-    total += (soups[s]->p.num_programs / 2 + kThreads - 1) / kThreads;
-  }
-  if (total > 0xffffffffull) return set_error(CUBFF_EINVAL, "batch_run: too many pairs");
-
-  const uint32_t chunk_max = static_cast<uint32_t>(std::min<uint64_t>(n_epochs, 1024));
-  CUBFF_TRY(eng->reserve_batch(size_t(chunk_max) * n_soups));
-  BatchDesc *hd = static_cast<BatchDesc *>(eng->h_desc);
-  BatchDesc *dd = static_cast<BatchDesc *>(eng->d_desc);
-  unsigned long long *dc = eng->d_bcnt, *hc = eng->h_bcnt;
-
-  uint64_t done = 0;
-  while (done < n_epochs) {
-    const uint32_t chunk = static_cast<uint32_t>(std::min<uint64_t>(chunk_max, n_epochs - done));
-    CUBFF_CUDA_TRY(cudaMemsetAsync(dc, 0, size_t(2) * chunk * n_soups * sizeof(unsigned long long), st));
-    for (uint32_t c = 0; c < chunk; c++) {
-      BatchDesc *row = hd + size_t(c) * n_soups;
-      for (int s = 0; s < n_soups; s++) {
-        cubff_soup *sp = soups[s];
-        const uint64_t e = sp->epoch + done + c;
-        if (sp->perm_count == 0 || e < sp->perm_first || e >= sp->perm_first + sp->perm_count) {
-          const uint64_t remaining = n_epochs - done - c;
-          CUBFF_TRY(sp->fill_pairing(e, static_cast<uint32_t>(std::min<uint64_t>(sp->batch, remaining))));
-        }
-        const uint64_t slot = e - sp->perm_first;
-        const uint64_t n = sp->p.num_programs;
-        EpochArgs &a = row[s].a;
-        a.soup = sp->d_soup;
-        a.perm = sp->d_perm + slot * n;
-        a.n = n;
-        a.num_indices = n / 2;
-        a.d_num_indices = sp->p.pairing == CUBFF_PAIR_PATTERN ? sp->d_num_indices + slot : nullptr;
-        a.epoch_key = seed_from(sp->s0, e);
-        a.mutation_prob = sp->p.mutation_prob;
-        a.ops = dc + (size_t(c) * n_soups + s) * 2;
-        a.raw = a.ops + 1;
-        row[s].lang = sp->p.lang;
-        row[s].block_begin = block_begin[s];
-      }
-      CUBFF_CUDA_TRY(cudaMemcpyAsync(dd + size_t(c) * n_soups, row, sizeof(BatchDesc) * n_soups,
-                                     cudaMemcpyHostToDevice, st));
-      CUBFF_TRY(launch_batch_epoch(dd + size_t(c) * n_soups, n_soups, static_cast<uint32_t>(total),
-                                   eng->device, st));
-      for (int s = 0; s < n_soups; s++) {
-        cubff_soup *sp = soups[s];
-        const uint64_t e = sp->epoch + done + c;
-        if (sp->p.reset_interval && e % sp->p.reset_interval == 0) {
-          if (done + c + 1 == n_epochs) sp->pending_reset = true;
-          else CUBFF_TRY(sp->apply_reset());
-        }
-      }
-    }
-    CUBFF_CUDA_TRY(cudaMemcpyAsync(hc, dc, size_t(2) * chunk * n_soups * sizeof(unsigned long long),
-                                   cudaMemcpyDeviceToHost, st));
-    CUBFF_CUDA_TRY(cudaStreamSynchronize(st));
-    for (uint32_t c = 0; c < chunk; c++)
-      for (int s = 0; s < n_soups; s++) ops[size_t(s) * n_epochs + done + c] = hc[(size_t(c) * n_soups + s) * 2];
-    done += chunk;
-  }
-  for (int s = 0; s < n_soups; s++) soups[s]->epoch += n_epochs;
-  return CUBFF_OK;
+  std::vector<uint64_t *> outs(n_soups);
+  for (int s = 0; s < n_soups; s++) outs[s] = ops ? ops + size_t(s) * n_epochs : nullptr;
+  return run_soups(eng, soups, n_soups, n_epochs, outs.data(), nullptr, nullptr);
 }

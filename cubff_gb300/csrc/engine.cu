@@ -92,7 +92,7 @@ static uint32_t pairing_batch(uint64_t n) {
   return static_cast<uint32_t>(std::min<uint64_t>(b, 64));
 }
 
-static constexpr uint32_t kCounterChunk = 4096;  // epochs of op counters per D2H
+static constexpr uint32_t kCounterChunk = cubff_soup::kCounterChunk;
 // Counter words: the pipelined runs keep kPipeCountSlots (ops, raw) pairs per
 // epoch; the per-epoch kernels one pair.
 static constexpr size_t kCounterWords = size_t(2) * kPipeCountSlots * kCounterChunk;
@@ -112,10 +112,7 @@ int cubff_soup::ensure_buffers() {
     CUBFF_CUDA_TRY(cudaMalloc(&d_mutmask, size_t(batch) * (p.num_programs / 2) * sizeof(uint4)));
     CUBFF_CUDA_TRY(cudaMalloc(&d_inv, size_t(batch) * p.num_programs * sizeof(uint32_t)));
     CUBFF_CUDA_TRY(cudaMalloc(&d_readycnt, size_t(batch) * (p.num_programs / 2) * sizeof(uint32_t)));
-    CUBFF_CUDA_TRY(cudaMalloc(&d_queue, size_t(batch) * (p.num_programs / 2) * sizeof(uint32_t)));
-    CUBFF_CUDA_TRY(cudaMalloc(&d_ctl, 4 * sizeof(uint32_t)));
-    CUBFF_CUDA_TRY(cudaMemset(d_ctl, 0, 4 * sizeof(uint32_t)));
-    CUBFF_CUDA_TRY(cudaMallocHost(&h_ctl, 4 * sizeof(uint32_t)));
+    CUBFF_CUDA_TRY(cudaMemset(d_readycnt, 0, size_t(batch) * (p.num_programs / 2) * sizeof(uint32_t)));
     perm_first = 0;
     perm_count = 0;
   }
@@ -133,14 +130,9 @@ void cubff_soup::release() {
   if (h_pat_perm) cudaFreeHost(h_pat_perm);
   if (d_inv) cudaFree(d_inv);
   if (d_readycnt) cudaFree(d_readycnt);
-  if (d_queue) cudaFree(d_queue);
-  d_inv = d_readycnt = d_queue = nullptr;
+  d_inv = d_readycnt = nullptr;
   if (d_mutmask) cudaFree(d_mutmask);
   d_mutmask = nullptr;
-  if (d_ctl) cudaFree(d_ctl);
-  if (h_ctl) cudaFreeHost(h_ctl);
-  d_ctl = nullptr;
-  h_ctl = nullptr;
   d_soup = nullptr;
   d_perm = nullptr;
   d_num_indices = nullptr;
@@ -151,8 +143,7 @@ void cubff_soup::release() {
 }
 
 // Computes the pairing of epochs [first, first + count) into d_perm.
-int cubff_soup::fill_pairing(uint64_t first, uint32_t count) {
-  cudaStream_t st = eng->stream;
+int cubff_soup::fill_pairing(uint64_t first, uint32_t count, cudaStream_t st) {
   const uint64_t n = p.num_programs;
   switch (p.pairing) {
     case CUBFF_PAIR_SHUFFLE:
@@ -187,6 +178,7 @@ int cubff_soup::fill_pairing(uint64_t first, uint32_t count) {
         });
       }
       for (auto &t : pool) t.join();
+      pat_ni.assign(hn, hn + count);
       CUBFF_CUDA_TRY(cudaMemcpyAsync(d_perm, hp, size_t(count) * n * sizeof(uint32_t),
                                      cudaMemcpyHostToDevice, st));
       CUBFF_CUDA_TRY(cudaMemcpyAsync(d_num_indices, hn, size_t(count) * sizeof(uint64_t),
@@ -203,110 +195,12 @@ int cubff_soup::fill_pairing(uint64_t first, uint32_t count) {
   return CUBFF_OK;
 }
 
-int cubff_soup::apply_reset() {
+int cubff_soup::apply_reset(cudaStream_t st) {
   const uint64_t n = p.num_programs;
-  CUBFF_TRY(launch_init(seed_from(s0, reset_index), n, d_soup, p.zero_init, (n / 32) * 32,
-                        eng->stream));
+  CUBFF_TRY(launch_init(seed_from(s0, reset_index), n, d_soup, p.zero_init, (n / 32) * 32, st));
   reset_index++;
   return CUBFF_OK;
 }
-
-int cubff_soup::run(uint64_t n_epochs, uint64_t *ops_out, uint64_t *raw_out, uint32_t *last_shuffle,
-                    uint64_t *ni_out) {
-  CUBFF_TRY(ensure_buffers());
-  cudaStream_t st = eng->stream;
-  const uint64_t n = p.num_programs;
-  if (pending_reset) {
-    CUBFF_TRY(apply_reset());
-    pending_reset = false;
-  }
-  uint64_t done = 0;
-  while (done < n_epochs) {
-    const uint32_t chunk = static_cast<uint32_t>(std::min<uint64_t>(kCounterChunk, n_epochs - done));
-    const size_t cwords = size_t(2) * kPipeCountSlots * chunk;
-    CUBFF_CUDA_TRY(cudaMemsetAsync(d_counters, 0, cwords * sizeof(unsigned long long), st));
-    uint32_t c = 0;
-    while (c < chunk) {
-      const uint64_t e = epoch + done + c;
-      if (perm_count == 0 || e < perm_first || e >= perm_first + perm_count) {
-        const uint64_t remaining = n_epochs - done - c;
-        CUBFF_TRY(fill_pairing(e, static_cast<uint32_t>(std::min<uint64_t>(batch, remaining))));
-      }
-      // One pipelined segment: within the cached pairings and the counter
-      // chunk, ending at the next reset epoch (a reset rewrites every program
-      // at once, common_language.h:590-595).
-      uint64_t seg = std::min<uint64_t>(chunk - c, perm_first + perm_count - e);
-      if (p.reset_interval) {
-        const uint64_t r = e + (p.reset_interval - e % p.reset_interval) % p.reset_interval;
-        seg = std::min<uint64_t>(seg, r - e + 1);
-      }
-      const uint64_t slot = e - perm_first;
-      CUBFF_CUDA_TRY(cudaMemsetAsync(d_readycnt, 0, seg * (n / 2) * sizeof(uint32_t), st));
-      CUBFF_CUDA_TRY(cudaMemsetAsync(d_queue, 0, seg * (n / 2) * sizeof(uint32_t), st));
-      CUBFF_CUDA_TRY(cudaMemsetAsync(d_ctl, 0, 2 * sizeof(uint32_t), st));  // queue head, tail
-      PipeArgs a;
-      a.soup = d_soup;
-      a.perm = d_perm + slot * n;
-      a.n = n;
-      a.s0 = s0;
-      a.e0 = e;
-      a.n_epochs = static_cast<uint32_t>(seg);
-      a.mutation_prob = p.mutation_prob;
-      a.d_num_indices = p.pairing == CUBFF_PAIR_PATTERN ? d_num_indices + slot : nullptr;
-      a.mutmask = d_mutmask + slot * (n / 2);
-      a.inv = d_inv + slot * n;
-      a.readycnt = d_readycnt;
-      a.queue = d_queue;
-      a.qctl = d_ctl;
-      a.error = reinterpret_cast<int *>(d_ctl + 2);
-      a.ops = d_counters + size_t(2) * kPipeCountSlots * c;
-      a.lanes_per_pair64 = eng->lanes_per_pair64;
-      CUBFF_TRY(launch_pipeline(p.lang, a, eng->device, st));
-      if (ni_out) {
-        if (p.pairing == CUBFF_PAIR_PATTERN)
-          CUBFF_CUDA_TRY(cudaMemcpyAsync(ni_out + done + c, d_num_indices + slot,
-                                         seg * sizeof(uint64_t), cudaMemcpyDeviceToHost, st));
-        else
-          for (uint64_t q = 0; q < seg; q++) ni_out[done + c + q] = n / 2;
-      }
-      const uint64_t last = e + seg - 1;
-      if (p.reset_interval && last % p.reset_interval == 0) {
-        if (done + c + seg == n_epochs) pending_reset = true;
-        else CUBFF_TRY(apply_reset());
-      }
-      c += static_cast<uint32_t>(seg);
-    }
-    CUBFF_CUDA_TRY(cudaMemcpyAsync(h_counters, d_counters, cwords * sizeof(unsigned long long),
-                                   cudaMemcpyDeviceToHost, st));
-    CUBFF_CUDA_TRY(cudaMemcpyAsync(h_ctl, d_ctl, 4 * sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
-    CUBFF_CUDA_TRY(cudaStreamSynchronize(st));
-    if (h_ctl[2] != 0) {
-      epoch += done;
-      return set_error(CUBFF_ETIMEDOUT,
-                       "soup_run: a pipelined epoch wait timed out; the soup state is invalid");
-    }
-    for (uint32_t q = 0; q < chunk; q++) {
-      uint64_t o = 0, r = 0;
-      for (int sl = 0; sl < kPipeCountSlots; sl++) {
-        o += h_counters[(size_t(q) * kPipeCountSlots + sl) * 2];
-        r += h_counters[(size_t(q) * kPipeCountSlots + sl) * 2 + 1];
-      }
-      if (ops_out) ops_out[done + q] = o;
-      if (raw_out) raw_out[done + q] = r;
-    }
-    done += chunk;
-  }
-  const uint64_t last = epoch + n_epochs - 1;
-  epoch += n_epochs;
-  if (n_epochs > 0 && last_shuffle) {
-    const uint64_t slot = last - perm_first;
-    CUBFF_CUDA_TRY(cudaMemcpyAsync(last_shuffle, d_perm + slot * n, n * sizeof(uint32_t),
-                                   cudaMemcpyDeviceToHost, st));
-    CUBFF_CUDA_TRY(cudaStreamSynchronize(st));
-  }
-  return CUBFF_OK;
-}
-
 
 extern "C" {
 
@@ -418,7 +312,7 @@ int cubff_engine_destroy(cubff_engine *engine) {
   if (!engine) return CUBFF_OK;
   cudaSetDevice(engine->device);
   cudaStreamSynchronize(engine->stream);
-  engine->release_batch();
+  engine->release_pipe();
   cudaStreamDestroy(engine->stream);
   delete engine;
   return CUBFF_OK;
@@ -459,6 +353,21 @@ int cubff_soup_create(cubff_engine *engine, const cubff_soup_params *params,
   }
   *out = s;
   return CUBFF_OK;
+}
+
+uint64_t cubff_soup_footprint_bytes(const cubff_soup_params *params) {
+  if (!params) return 0;
+  const uint64_t n = params->num_programs, P = n / 2;
+  const uint64_t batch = pairing_batch(n);
+  uint64_t bytes = n * kTape;                                     // the soup
+  bytes += batch * n * sizeof(uint32_t) + batch * sizeof(uint64_t);  // pairings, num_indices
+  if (params->pairing == CUBFF_PAIR_SHUFFLE) bytes += shuffle_scratch_bytes(n, batch);
+  bytes += kCounterWords * sizeof(unsigned long long);            // op counters
+  bytes += batch * P * sizeof(uint4);                             // mutation masks
+  bytes += batch * n * sizeof(uint32_t);                          // inverse shuffles
+  bytes += batch * P * sizeof(uint32_t);                          // ready counters
+  bytes += batch * P * sizeof(uint32_t);                          // ready-queue share
+  return bytes;
 }
 
 int cubff_soup_destroy(cubff_soup *soup) {
@@ -537,7 +446,18 @@ int cubff_soup_run(cubff_soup *soup, uint64_t n_epochs, uint64_t *ops_per_epoch,
   if (soup->p.pairing == CUBFF_PAIR_PATTERN && soup->pat_offs.empty())
     return set_error(CUBFF_EINVAL, "soup_run: pattern pairing needs cubff_soup_set_pattern");
   CUBFF_CUDA_TRY(cudaSetDevice(soup->eng->device));
-  return soup->run(n_epochs, ops_per_epoch, raw_per_epoch, last_shuffle, num_indices_per_epoch);
+  CUBFF_TRY(run_soups(soup->eng, &soup, 1, n_epochs, &ops_per_epoch, &raw_per_epoch,
+                      &num_indices_per_epoch));
+  if (n_epochs > 0 && last_shuffle) {
+    // run_soups leaves the last epoch's pairing cached.
+    const uint64_t n = soup->p.num_programs;
+    const uint64_t slot = soup->epoch - 1 - soup->perm_first;
+    cudaStream_t st = soup->eng->stream;
+    CUBFF_CUDA_TRY(cudaMemcpyAsync(last_shuffle, soup->d_perm + slot * n, n * sizeof(uint32_t),
+                                   cudaMemcpyDeviceToHost, st));
+    CUBFF_CUDA_TRY(cudaStreamSynchronize(st));
+  }
+  return CUBFF_OK;
 }
 
 int cubff_soup_selfrep(cubff_soup *soup, uint64_t epoch, uint64_t *result) {

@@ -13,12 +13,21 @@ struct cubff_engine {
   cudaStream_t stream = nullptr;
   uint32_t lanes_per_pair64 = 0;  // pipelined-run lanes in flight per 64 pairs (0 = default)
 
-  // Batched-epoch staging (batch.cu): per-epoch soup descriptors and counters.
-  void *d_desc = nullptr, *h_desc = nullptr;
-  unsigned long long *d_bcnt = nullptr, *h_bcnt = nullptr;
-  size_t desc_cap = 0;  // descriptors
-  int reserve_batch(size_t n_desc);
-  void release_batch();
+  // Pipelined runs (batch.cu).  A run splits its soups into launch groups
+  // (one language, at most kMaxPipeSoups soups); group g runs on streams[g],
+  // owns a slice of the ready-queue entries d_queue and words [4g, 4g + 4) of
+  // d_ctl: queue head, tail, error flag.  The queue entries and the soups'
+  // ready counters are zero between launches; `dirty` says a launch gave up
+  // and may have left them otherwise.
+  std::vector<cudaStream_t> streams;
+  std::vector<cudaEvent_t> events;  // [0] fork, [1 + g] group g done
+  uint32_t *d_queue = nullptr;
+  size_t queue_cap = 0;              // entries
+  uint32_t *d_ctl = nullptr, *h_ctl = nullptr;
+  size_t ctl_groups = 0;
+  bool dirty = false;
+  int reserve_pipe(size_t groups, size_t queue_entries);
+  void release_pipe();
 };
 
 struct cubff_soup {
@@ -39,17 +48,19 @@ struct cubff_soup {
   void *d_scratch = nullptr;
   size_t scratch_bytes = 0;
   uint64_t *h_pat_perm = nullptr;  // pinned staging for host pattern pairings
+  std::vector<uint64_t> pat_ni;    // num_indices of the cached pattern pairings
 
-  // Pipelined runs (pipeline.cu): ready-queue state, and the queue head/tail +
-  // error flag of the current launch (d_ctl).
+  // Pipelined runs: inverse shuffles, mutation masks and ready counters of
+  // the cached epochs (the counters are zero between launches).
   uint32_t *d_inv = nullptr;       // [batch][num_programs] inverse shuffles
   uint32_t *d_readycnt = nullptr;  // [batch][num_programs / 2] ready-queue input counts
-  uint32_t *d_queue = nullptr;     // [batch][num_programs / 2] ready queue
-  uint4 *d_mutmask = nullptr;  // [batch][num_programs / 2] mutation masks
-  uint32_t *d_ctl = nullptr;
-  uint32_t *h_ctl = nullptr;
+  uint4 *d_mutmask = nullptr;      // [batch][num_programs / 2] mutation masks
 
-  // Per-epoch op / raw-step counters.
+  bool dirty = false;              // a launch gave up: d_readycnt may be nonzero
+
+  // Per-epoch op / raw-step counters: kPipeCountSlots (ops, raw) pairs for
+  // each of kCounterChunk epochs, reduced on the host.
+  static constexpr uint32_t kCounterChunk = 4096;
   unsigned long long *d_counters = nullptr;
   unsigned long long *h_counters = nullptr;
 
@@ -57,12 +68,16 @@ struct cubff_soup {
 
   int ensure_buffers();
   void release();
-  int fill_pairing(uint64_t first, uint32_t count);
-  int apply_reset();
-  int run(uint64_t n_epochs, uint64_t *ops_out, uint64_t *raw_out, uint32_t *last_shuffle,
-          uint64_t *ni_out);
+  int fill_pairing(uint64_t first, uint32_t count, cudaStream_t st);
+  int apply_reset(cudaStream_t st);
 };
 
 namespace cubff {
 using Soup = cubff_soup;
+
+// Advances every soup by n_epochs epochs in pipelined launches (batch.cu).
+// ops / raw / ni: per-soup host arrays of n_epochs entries (each nullable):
+// op count, raw interpreter iterations and evaluated pairs of each epoch.
+int run_soups(cubff_engine *eng, cubff_soup *const *soups, int n_soups, uint64_t n_epochs,
+              uint64_t *const *ops, uint64_t *const *raw, uint64_t *const *ni);
 }

@@ -43,30 +43,50 @@ struct EpochArgs {
   unsigned long long *raw;              // += raw iterations (nullable)
 };
 
-// Launch arguments of a pipelined run of epochs [e0, e0 + n_epochs) of one
-// soup (pipeline.cu).
-struct PipeArgs {
+// A pipelined launch runs epochs of one or more soups (pipeline.cu).  Soups
+// are listed grouped by language; each language has one ready queue.
+struct PipeSoup {
   uint8_t *soup;
-  const uint32_t *perm;                 // [n_epochs][n] shuffle_idx
-  uint64_t n;
-  uint64_t s0;                          // SplitMix64(params.seed)
-  uint64_t e0;
-  uint32_t n_epochs;
-  uint32_t mutation_prob;
-  const uint64_t *d_num_indices;        // [n_epochs] or nullptr (= n / 2)
-  const uint4 *mutmask;                 // [n_epochs][n / 2] mutation masks
-  const uint32_t *inv;                  // [n_epochs][n] position of program p in perm
-  uint32_t *readycnt;                   // [n_epochs][n / 2] inputs published, zeroed
-  uint32_t *queue;                      // [(n_epochs - 1) * n / 2] ready tasks + 1, zeroed
-  uint32_t *qctl;                       // [0] head, [1] tail; zeroed
-  int *error;                           // set when a bounded wait gives up
-  unsigned long long *ops;              // [n_epochs][kCountSlots][2]: ops, raw
-  uint32_t lanes_per_pair64;            // lanes per 64 pairs of an epoch (0 = default)
+  const uint32_t *perm;         // [E][n] shuffle_idx of epochs e0 .. e0 + E - 1
+  const uint32_t *inv;          // [E][n] position of program p in perm
+  const uint4 *mutmask;         // [E][n / 2] mutation masks
+  uint32_t *readycnt;           // [E][n / 2] inputs published; zero, left zero
+  const uint64_t *num_indices;  // [E] evaluated pairs, or nullptr (= n / 2)
+  unsigned long long *ops;      // [E][kPipeCountSlots][2] ops, raw; zeroed
+  uint64_t n, s0, e0;           // s0 = SplitMix64(params.seed)
+  uint32_t npairs, mutation_prob;
+  uint32_t task_base;           // first task id: sum of npairs * E over earlier soups
+  uint32_t init_base;           // sum of npairs over earlier soups of the same language
+  int lang;
+  uint32_t n_epochs;            // E: epochs of this soup in the launch
+};
+
+struct PipeQueue {
+  uint32_t *queue;              // ready tasks + 1; total - initial entries, zero, left zero
+  uint32_t *ctl;                // [0] head, [1] tail; zeroed
+  uint32_t total, initial;      // tasks of this language; those of the first epoch
+  uint32_t first_soup, n_soups;
+  int lang;
+};
+
+// Everything a pipelined launch needs, passed by value as the kernel's
+// (grid-constant) parameter, so that a launch needs no host-to-device copy
+// and can be captured in a CUDA graph.  All soups have the queue's language;
+// the queue serves soups [first_soup, first_soup + n_soups) = all of them.
+constexpr int kMaxPipeSoups = 128;
+struct PipeBatch {
+  PipeSoup soups[kMaxPipeSoups];
+  PipeQueue queue;
+  int n_soups;
+  int *error;                   // set when a bounded wait gives up
 };
 constexpr int kPipeCountSlots = 32;
 
 // Launchers (epoch.cu / pairing.cu / pipeline.cu).
-int launch_pipeline(int lang, const PipeArgs &a, int device, cudaStream_t stream);
+// total_pairs = pairs of one epoch over all soups; lanes_per_pair64 = lanes
+// in flight per 64 of them (0 = default).
+int launch_pipeline(const PipeBatch &b, uint64_t total_pairs, uint32_t lanes_per_pair64,
+                    int device, cudaStream_t stream);
 int launch_mutation_masks(uint64_t s0, uint64_t e0, uint32_t n_epochs, uint64_t n, uint32_t prob,
                           uint4 *out, cudaStream_t stream);
 int launch_inverse(const uint32_t *perm, uint32_t n_epochs, uint64_t n, uint32_t *inv,

@@ -13,8 +13,9 @@
  *   2. Device-resident soups: the epoch loop of Simulation<L>::RunSimulation
  *      (common_language.h:345-596) minus the host callback, which the C++ /
  *      Python layers above drive.
- *   3. Batching (many soups, one launch per epoch) and serving (continuous
- *      admission of soup jobs by device-memory footprint).
+ *   3. Batching (many soups advanced together in shared pipelined launches)
+ *      and serving (continuous admission of soup jobs by device-memory
+ *      footprint, on a worker thread).
  *
  * Language ids follow the reference's registered names (see
  * cubff_language_name); pairing modes follow common_language.h:433-486.
@@ -213,13 +214,65 @@ int cubff_eval_pair(int lang, uint8_t *tape, uint64_t *ops, uint64_t *raw);
 int cubff_eval_selfrep(int lang, const uint8_t *program, uint64_t epoch_key,
                        uint64_t *result);
 
+/* Device memory a soup with these parameters holds once it has run: the
+ * soup, its cached pairings (perm, inverse, mutation masks, ready counters),
+ * pairing scratch, op counters and its share of the ready queue. */
+uint64_t cubff_soup_footprint_bytes(const cubff_soup_params *params);
+
 /* ---- layer 3: batching ------------------------------------------------- */
-/* Advances every soup by n_epochs epochs; each epoch of all soups is one
- * kernel launch (persistent, soup-descriptor driven) captured in a CUDA graph.
- * ops: host array [n_soups][n_epochs].  Every soup must belong to engine and
- * use CUBFF_PAIR_SHUFFLE, FIXED or CYCLIC. */
+/* Advances every soup by n_epochs epochs, as cubff_soup_run does for each
+ * (same results, soup for soup), but all soups together: soups of one
+ * language share persistent pipelined launches (up to 128 soups per launch),
+ * and the launches of different languages run on streams of their own.
+ * ops: host array [n_soups][n_epochs].  Every soup must belong to engine;
+ * pattern-paired soups need their interaction lists. */
 int cubff_batch_run(cubff_engine *engine, cubff_soup **soups, int n_soups,
                     uint64_t n_epochs, uint64_t *ops);
+
+/* ---- layer 4: serving -------------------------------------------------- */
+/* A server runs soup jobs (parameters + epoch count) submitted at any time.
+ * A worker thread admits queued jobs in submission order while the summed
+ * footprint (cubff_soup_footprint_bytes) of the running jobs stays within
+ * hbm_budget_bytes, advances all running jobs together (cubff_batch_run) in
+ * rounds of at most round_epochs epochs, and retires finished jobs: their
+ * final soup and per-epoch op counts are kept on the host until fetched.  A
+ * job's results are the same as cubff_soup_run's on a soup created with the
+ * same parameters.  The worker owns the engine: do not use the engine, or
+ * its soups, while the server exists. */
+typedef struct cubff_server cubff_server;
+
+typedef struct {
+  uint64_t job_id;
+  int status;           /* CUBFF_OK, or the error that ended the job      */
+  uint64_t num_programs;
+  uint64_t n_epochs;
+  uint64_t total_ops;   /* sum of the per-epoch op counts                 */
+  double submit_s;      /* seconds since the server was created           */
+  double start_s;       /* admitted                                       */
+  double finish_s;      /* results on the host                            */
+} cubff_job_info;
+
+/* round_epochs = 0 picks 64. */
+int cubff_server_create(cubff_engine *engine, uint64_t hbm_budget_bytes,
+                        uint32_t round_epochs, cubff_server **out);
+/* Stops the worker after its current round; unfinished jobs are dropped. */
+int cubff_server_destroy(cubff_server *server);
+/* Queues a job.  CUBFF_EINVAL for bad parameters or a job whose footprint
+ * alone exceeds the budget.  Pattern pairing is not served. */
+int cubff_server_submit(cubff_server *server, const cubff_soup_params *params,
+                        uint64_t n_epochs, uint64_t *job_id);
+/* Up to max_jobs jobs finished since the last poll, each reported once;
+ * waits up to wait_s seconds for the first one.  *n_out = jobs written. */
+int cubff_server_poll(cubff_server *server, cubff_job_info *out, int max_jobs,
+                      int *n_out, double wait_s);
+/* Copies a finished job's soup (num_programs * 64 bytes; nullable) and
+ * per-epoch op counts (n_epochs entries; nullable), then forgets the job.
+ * CUBFF_ENOTFOUND for an unknown, unfinished or already fetched job. */
+int cubff_server_fetch(cubff_server *server, uint64_t job_id, uint8_t *soup_out,
+                       uint64_t *ops_out);
+/* Jobs queued, running, and finished but not fetched; device bytes held. */
+int cubff_server_stats(cubff_server *server, uint64_t *queued, uint64_t *running,
+                       uint64_t *finished, uint64_t *hbm_bytes);
 
 #ifdef __cplusplus
 }
