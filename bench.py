@@ -346,6 +346,9 @@ def cpu_sample(budget_s: float = 15.0, max_epochs: int = 10**9):
 
 
 DRAW_OPS = 21  # 32-bit integer ops of one SplitMix64 mutation draw + its threshold test
+# DRAM traffic of one 64-epoch pipelined launch of this workload (2^17 programs), from an ncu
+# capture: dram__bytes_read.sum + dram__bytes_write.sum = 175.4 MB + 24.7 MB.
+NCU_DRAM_BYTES_PER_LAUNCH = 200.2e6
 
 
 def roofline(gv, peaks, peaks_src, sm_mhz):
@@ -370,7 +373,10 @@ def roofline(gv, peaks, peaks_src, sm_mhz):
     work = float(gv["raw"].astype(float).sum()) * K_LANG[LANG] + (N // 2) * 128.0 * DRAW_OPS * epochs
     achieved = work / kern_s / 1e12
     return {"bound": "int_issue", "achieved": achieved, "peak": peak, "unit": "Tintop/s",
-            "frac": achieved / peak, "traffic": None,
+            "frac": achieved / peak,
+            "traffic": NCU_DRAM_BYTES_PER_LAUNCH if N == 1 << 17 else None,
+            "traffic_unit": "bytes per 64-epoch launch (ncu capture)",
+            "algorithmic_bytes_per_launch": 264.0 * (N // 2) * 64,
             "peak_source": f"{sms} SMs x 128 x {clk:.0f} MHz ({peaks_src} sm_max_mhz)",
             "work_per_launch_Tintop": work / len(gv["kern_ms"]) / 1e12,
             "launch_mean_ms": kern_s * 1e3 / len(gv["kern_ms"]),
