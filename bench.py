@@ -37,6 +37,8 @@ REPO = os.path.dirname(os.path.abspath(__file__))
 if REPO not in sys.path:
     sys.path.insert(0, REPO)
 
+from cubff_gb300 import replicas  # noqa: E402  (pure Python; no CUDA needed to import)
+
 LANG = "bff_noheads"
 N = 1 << 17
 SEED = 1
@@ -63,11 +65,6 @@ def parse():
     return ap.parse_args()
 
 
-def dist_info():
-    rank = int(os.environ.get("RANK", "0"))
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    return rank, world, local
 
 
 def measured_peaks():
@@ -131,7 +128,8 @@ class ClockSampler:
 # ---------------------------------------------------------------------------
 # Our arm.
 
-def gpu_value(torch, abi, steps: int, warmup: int, sm_mhz_hint: float):
+def gpu_value(torch, abi, steps: int, warmup: int, sm_mhz_hint: float, seed: int = SEED,
+              group=None):
     """Device time of the epochs through the kernel-level C ABI on a torch
     stream: per segment of 64 epochs, cubff_shuffle_indices (pairing) and
     cubff_run_epochs (the pipelined epochs), bracketed by CUDA events on that
@@ -159,11 +157,11 @@ def gpu_value(torch, abi, steps: int, warmup: int, sm_mhz_hint: float):
                 flush.fill_(done & 0xFF)  # evict the previous segment from L2
                 ev.append([torch.cuda.Event(enable_timing=True) for _ in range(3)])
                 ev[-1][0].record(stream)
-            abi.check(L.cubff_shuffle_indices(SEED, e, seg, N, perm.data_ptr(), scratch.data_ptr(),
+            abi.check(L.cubff_shuffle_indices(seed, e, seg, N, perm.data_ptr(), scratch.data_ptr(),
                                               scratch.numel(), sp))
             if timed:
                 ev[-1][1].record(stream)
-            abi.check(L.cubff_run_epochs(lang, soup.data_ptr(), perm.data_ptr(), None, SEED, e, seg,
+            abi.check(L.cubff_run_epochs(lang, soup.data_ptr(), perm.data_ptr(), None, seed, e, seg,
                                          MUT, N, counters.data_ptr() + 16 * done, ws.data_ptr(),
                                          ws.numel(), sp))
             if timed:
@@ -174,17 +172,19 @@ def gpu_value(torch, abi, steps: int, warmup: int, sm_mhz_hint: float):
 
     with torch.cuda.stream(stream):
         wsoup = torch.empty(N * 64, dtype=torch.uint8, device=dev)
-        abi.check(L.cubff_init_programs(seed_of(SEED, 0), N, wsoup.data_ptr(), 0, N, sp))
+        abi.check(L.cubff_init_programs(seed_of(seed, 0), N, wsoup.data_ptr(), 0, N, sp))
         wcnt = torch.zeros(max(warmup, 1) * 2, dtype=torch.int64, device=dev)
         run(wsoup, 0, warmup, wcnt, False)
         stream.synchronize()
         soup = torch.empty(N * 64, dtype=torch.uint8, device=dev)
-        abi.check(L.cubff_init_programs(seed_of(SEED, 0), N, soup.data_ptr(), 0, N, sp))
+        abi.check(L.cubff_init_programs(seed_of(seed, 0), N, soup.data_ptr(), 0, N, sp))
         counters = torch.zeros(steps * 2, dtype=torch.int64, device=dev)
         stream.synchronize()
+        replicas.barrier(group)
         launches["n"] = 0
         ev = run(soup, 0, steps, counters, True)
         stream.synchronize()
+        replicas.barrier(group)
         abi.check(L.cubff_run_epochs_status(ws.data_ptr(), N, B, sp))
     seg_ms = [x.elapsed_time(z) for x, y, z in ev]
     kern_ms = [y.elapsed_time(z) for x, y, z in ev]
@@ -194,28 +194,30 @@ def gpu_value(torch, abi, steps: int, warmup: int, sm_mhz_hint: float):
             "raw": raw, "soup": soup.cpu().numpy(), "launches": launches["n"], "segments": len(ev)}
 
 
-def gpu_e2e(torch, abi, steps: int):
+def gpu_e2e(torch, abi, steps: int, seed: int = SEED, group=None):
     """The same epochs through the soup-level C ABI with host buffers:
     H2D of the initial soup, cubff_soup_run (per-epoch op counts back to the
     host), D2H of the final soup, wall clock."""
     import numpy as np
     eng = abi.Engine(0)
-    ref = abi.Soup(eng, LANG, N, SEED, MUT)
+    ref = abi.Soup(eng, LANG, N, seed, MUT)
     init = torch.from_numpy(ref.read()).pin_memory()
     ref.close()
     out = torch.empty(N * 64, dtype=torch.uint8).pin_memory()
-    soup = abi.Soup(eng, LANG, N, SEED, MUT)
+    soup = abi.Soup(eng, LANG, N, seed, MUT)
     soup.run(1)  # allocate the pairing buffers outside the timed region
     soup.set_epoch(0, 1)
     ops = np.zeros(steps, dtype=np.uint64)
     raw = np.zeros(steps, dtype=np.uint64)
     torch.cuda.synchronize()
+    replicas.barrier(group)
     t0 = time.perf_counter()
     abi.check(abi.lib().cubff_soup_write(soup.h, init.data_ptr(), 0, N * 64))
     abi.check(abi.lib().cubff_soup_run(soup.h, steps, ops.ctypes.data, raw.ctypes.data, None, None))
     abi.check(abi.lib().cubff_soup_read(soup.h, out.data_ptr(), 0, N * 64))
     torch.cuda.synchronize()
     dt = time.perf_counter() - t0
+    replicas.barrier(group)
     soup.close()
     eng.close()
     return {"total_s": dt, "ops": ops, "raw": raw, "soup": out.numpy().copy()}
@@ -386,7 +388,7 @@ def roofline(gv, peaks, peaks_src, sm_mhz):
 
 def main():
     args = parse()
-    rank, world, local = dist_info()
+    rank, world, local = replicas.env()
     if args.impl == "reference":
         if rank != 0:
             return
@@ -405,38 +407,49 @@ def main():
     import torch
     from cubff_gb300 import abi
     torch.cuda.set_device(local)
+    group = replicas.init()
+    seed = replicas.replica_seed(SEED, rank)  # independent replicas: one soup per GPU
     abi.lib()
     peaks, src = measured_peaks()
     with ClockSampler(local) as clocks:
-        gv = gpu_value(torch, abi, args.steps, args.warmup, peaks.get("sm_max_mhz", 2070.0))
+        gv = gpu_value(torch, abi, args.steps, args.warmup, peaks.get("sm_max_mhz", 2070.0),
+                       seed, group)
     ck = clocks.summary()
-    e2 = gpu_e2e(torch, abi, args.steps)
+    e2 = gpu_e2e(torch, abi, args.steps, seed, group)
     assert np.array_equal(gv["ops"], e2["ops"]) and np.array_equal(gv["soup"], e2["soup"]), \
         "kernel-level and soup-level paths disagree"
-    ops_total = float(gv["ops"].sum())
-    value = ops_total / gv["total_s"] * world
-    line = {"metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": world,
+    # Work summed over ranks, time maximised over ranks.
+    ops_all, t_dev = replicas.reduce(float(gv["ops"].sum()), gv["total_s"], group)
+    raw_all, _ = replicas.reduce(float(gv["raw"].sum()), gv["total_s"], group)
+    ops_e2e, t_e2e = replicas.reduce(float(e2["ops"].sum()), e2["total_s"], group)
+    line = {"metric": METRIC, "value": ops_all / t_dev, "unit": "steps/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": gv["total_s"] * 1e3 / args.steps, "higher_is_better": True,
+            "ms_per_step": t_dev * 1e3 / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "u8",
             "data": "synthetic (seeded reference init)", "config": CONFIG,
-            "raw_steps_per_s": float(gv["raw"].sum()) / gv["total_s"] * world,
-            "pairs_per_s": (N // 2) * args.steps / gv["total_s"] * world,
+            "raw_steps_per_s": raw_all / t_dev,
+            "pairs_per_s": (N // 2) * args.steps * world / t_dev,
             "gpu_launches": gv["launches"],
             "roofline": roofline(gv, peaks, src, ck.get("sm_mhz")),
             "clocks": ck,
-            "e2e": {"value": ops_total / e2["total_s"], "unit": "steps/s",
+            "e2e": {"value": ops_e2e / t_e2e, "unit": "steps/s",
                     "h2d_bytes_per_step": N * 64 / args.steps,
                     "d2h_bytes_per_step": (N * 64 + 16 * args.steps) / args.steps,
-                    "wall_s": e2["total_s"]}}
-    if not args.no_batch:
+                    "wall_s": t_e2e}}
+    if world > 1:
+        line["replicas"] = f"{world} independent soups (seeds {SEED}..{SEED + world - 1}), one per GPU"
+    if rank == 0 and not args.no_batch:
         line["batched"] = batch_compare(torch, abi, 64)
-    if not args.no_serving:
+    if rank == 0 and not args.no_serving:
         line["serving"] = serving_sample(torch, abi, args.serving_jobs)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_sample()
     if rank == 0:
         print(json.dumps(line))
+    if group is not None:
+        replicas.barrier(group)
+        import torch.distributed as dist
+        dist.destroy_process_group()
 
 
 if __name__ == "__main__":
