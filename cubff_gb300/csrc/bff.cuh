@@ -25,6 +25,15 @@
 //    repeats with that head shifted by the same amount each time; k
 //    repetitions advance i by k*P, nskip by k times the segment's skips and
 //    the head by k times its shift (mod 128).
+//
+// Fast mode.  A pair that is still running after kFastAfter steps switches,
+// when the caller provides a next-command array (LaneNp), to a mode in which
+// one 16-bit entry per position gives the next command position >= p and its
+// op (entry = q << 4 | op, q = 128 when none): a step's fetch and no-op run
+// are one shared-memory load, issued one step ahead.  The bytes under the two
+// heads are cached in registers (v0, v1).  Writes that change a byte's op
+// rewrite the entries of the positions whose next command it is.  Both modes
+// share all other state, so the switch changes nothing in the results.
 #pragma once
 
 #include "cycle.cuh"
@@ -34,10 +43,16 @@ namespace cubff {
 
 enum BffLogic { kLogicScan, kLogicJump8, kLogicSelfmove };
 
+constexpr uint32_t kFastAfter = 32;  // basic-mode steps before the switch
+
 template <bool kHeads, int kLogic, uint32_t kNullMask>
 struct BffMachine {
   int pc, h0, h1;
   uint32_t i, nskip, mods;
+  uint32_t nbasic;    // steps taken in basic mode
+  bool fast;          // fast mode: np holds the next-command entries
+  uint32_t v0, v1;    // fast mode: tape[h0], tape[h1]
+  uint32_t nxt;       // fast mode: np entry of pc, loaded one step ahead
   bool have_brk;
   bool used0, used1;  // heads used as addresses since the snapshot
   Mask128 cmd, opn, cls;
@@ -59,6 +74,9 @@ struct BffMachine {
       pc = 0;
     }
     i = nskip = mods = 0;
+    nbasic = 0;
+    fast = false;
+    v0 = v1 = nxt = 0;
     used0 = used1 = false;
     touched = Mask128{0, 0};
     s_pc = -1;
@@ -145,10 +163,172 @@ struct BffMachine {
     }
   }
 
+  // Fast mode: builds the next-command entries and the bracket masks, loads
+  // the head caches and the entry of pc.
+  __host__ __device__ __forceinline__ void enter_fast(const LaneBytes t, const LaneNp np,
+                                                      const uint8_t *__restrict__ optab) {
+    if (!have_brk) build_brackets(t, optab);
+    uint32_t e = uint32_t(kPair) << 4;
+    np.set(kPair, e);
+    for (int p = kPair - 1; p >= 0; p--) {
+      if (mask_test(cmd, p)) e = (uint32_t(p) << 4) | optab[t.get(p)];
+      np.set(p, e);
+    }
+    v0 = t.get(h0);
+    v1 = t.get(h1);
+    nxt = np.get(pc);
+    fast = true;
+  }
+
+  // write() for fast mode: also rewrites the next-command entries of the
+  // positions after the previous command up to a when a's op changes.
+  // Returns true when entries changed (the prefetched entry may be stale).
+  __host__ __device__ __forceinline__ bool write_fast(const LaneBytes t, const LaneBytes snapa,
+                                                      const LaneNp np,
+                                                      const uint8_t *__restrict__ optab, int a,
+                                                      uint32_t o, uint32_t v) {
+    if (v == o) return false;
+    t.set(a, v);
+    mods++;
+    if (!mask_test(touched, a)) {
+      mask_assign(touched, a, true);
+      snapa.set(a, o);
+    }
+    const uint32_t co = optab[o], cn = optab[v];
+    if (co == cn) return false;
+    const bool is = cn < kNull, was = co < kNull;
+    mask_assign(opn, a, cn == kLoopStart);
+    mask_assign(cls, a, cn == kLoopEnd);
+    if (!is && !was) return false;
+    mask_assign(cmd, a, is);
+    const uint32_t ent = is ? ((uint32_t(a) << 4) | cn) : np.get(a + 1);
+    const int lo = mask_prev(cmd, a - 1) + 1;
+    for (int p = a; p >= lo; p--) np.set(p, ent);
+    return true;
+  }
+
+  __host__ __device__ __forceinline__ bool step_fast(const LaneBytes t, const LaneBytes snapa,
+                                                     const LaneNp np,
+                                                     const uint8_t *__restrict__ optab) {
+    const uint32_t e = nxt;
+    const int q = static_cast<int>(e >> 4);
+    const uint32_t run = static_cast<uint32_t>(q - pc);
+    if (run) {
+      if (i + run >= kStepLimit) {
+        nskip += kStepLimit - i;
+        i = kStepLimit;
+        return true;
+      }
+      i += run;
+      nskip += run;
+      pc = q;
+      if (pc >= kPair) return true;
+    }
+    const uint32_t c = e & 15;
+    int npc = pc + 1;
+    nxt = np.get(npc);  // npc <= kPair: the sentinel entry exists
+    bool back = false;
+    if (c >= kDec0) {
+      if (c <= kInc0) {
+        h0 = (h0 + (c == kInc0 ? 1 : -1)) & (kPair - 1);
+        v0 = t.get(h0);
+      } else {
+        h1 = (h1 + (c == kInc1 ? 1 : -1)) & (kPair - 1);
+        v1 = t.get(h1);
+      }
+    } else if (c >= kPlus) {
+      used0 = true;
+      const bool to1 = c == kCopy01;
+      if (c >= kCopy01) used1 = true;
+      const int a = to1 ? h1 : h0;
+      const uint32_t o = to1 ? v1 : v0;
+      const uint32_t v = (c == kPlus ? v0 + 1 : c == kMinus ? v0 - 1 : to1 ? v0 : v1) & 0xFF;
+      if (to1) v1 = v; else v0 = v;
+      if (h0 == h1) v0 = v1 = v;
+      if (write_fast(t, snapa, np, optab, a, o, v)) nxt = np.get(npc);
+      if (kLogic == kLogicSelfmove && c == kCopy10) {
+        h1 = (h1 + 1) & (kPair - 1);
+        v1 = t.get(h1);
+      }
+    } else if (c == kLoopStart) {
+      used0 = true;
+      if ((v0 & kNullMask) == 0) {
+        if (kLogic == kLogicJump8) {
+          pc += 8;
+        } else {
+          const Mask128 brk{opn.lo | cls.lo, opn.hi | cls.hi};
+          int depth = 1, p = pc + 1;
+          while (true) {
+            const int b = mask_next(brk, p);
+            if (b >= kPair) { pc = kPair; break; }
+            depth += mask_test(opn, b) ? 1 : -1;
+            if (depth == 0) { pc = b; break; }
+            p = b + 1;
+          }
+        }
+        npc = pc + 1;
+        if (npc <= kPair) nxt = np.get(npc);
+      }
+    } else {
+      used0 = true;
+      if ((v0 & kNullMask) != 0) {
+        back = true;
+        if (kLogic == kLogicJump8) {
+          pc -= 8;
+        } else {
+          const Mask128 brk{opn.lo | cls.lo, opn.hi | cls.hi};
+          int depth = 1, p = pc - 1;
+          while (true) {
+            const int b = mask_prev(brk, p);
+            if (b < 0) { pc = -1; break; }
+            depth += mask_test(cls, b) ? 1 : -1;
+            if (depth == 0) { pc = b; break; }
+            p = b - 1;
+          }
+        }
+        npc = pc + 1;
+        if (npc >= 0) nxt = np.get(npc);
+      }
+    }
+    i++;
+    if (pc < 0) return true;
+    pc = npc;
+    if (pc >= kPair || i >= kStepLimit) return true;
+    if (back) {
+      const int g0 = h0, g1 = h1;
+      visit(t, snapa);
+      if (i >= kStepLimit) return true;
+      if (h0 != g0) v0 = t.get(h0);
+      if (h1 != g1) v1 = t.get(h1);
+    }
+    return false;
+  }
+
+  // Fast mode only (the pipelined kernel): the first step builds the
+  // next-command entries.
+  __host__ __device__ __forceinline__ bool step_lane(const LaneBytes t, const LaneBytes snapa,
+                                                     const LaneNp np,
+                                                     const uint8_t *__restrict__ optab) {
+    if (!fast) enter_fast(t, np, optab);
+    return step_fast(t, snapa, np, optab);
+  }
+
   // One step: a run of no-ops (if any) and then one command.  Returns true
-  // when the program has ended; the op count is then i - nskip.
+  // when the program has ended; the op count is then i - nskip.  np may have
+  // no array (np.s == nullptr): the machine then stays in basic mode.
   __host__ __device__ __forceinline__ bool step(const LaneBytes t, const LaneBytes snapa,
+                                                const LaneNp np,
                                                 const uint8_t *__restrict__ optab) {
+    if (fast) return step_fast(t, snapa, np, optab);
+    if (np.s && ++nbasic > kFastAfter) {
+      enter_fast(t, np, optab);
+      return step_fast(t, snapa, np, optab);
+    }
+    return step_basic(t, snapa, optab);
+  }
+
+  __host__ __device__ __forceinline__ bool step_basic(const LaneBytes t, const LaneBytes snapa,
+                                                      const uint8_t *__restrict__ optab) {
     const int q = mask_next(cmd, pc);
     const uint32_t run = static_cast<uint32_t>(q - pc);
     if (run) {
@@ -252,7 +432,7 @@ __host__ __device__ __forceinline__ uint32_t bff_eval(const LaneBytes t, const L
                                                       uint32_t *raw) {
   BffMachine<kHeads, kLogic, kNullMask> m;
   m.begin(t, bff_command_mask(t, optab));
-  while (!m.step(t, snapa, optab)) {
+  while (!m.step_basic(t, snapa, optab)) {
   }
   *raw = m.raw();
   return m.ops();

@@ -69,4 +69,21 @@ struct LaneBytes {
   }
 };
 
+// One thread's array of kPair + 1 16-bit entries (the BFF next-command
+// array, bff.cuh).  Entry p of thread tid sits at element p * 128 + tid of a
+// block of 128 threads: a warp's 32 lanes read 64 consecutive bytes for any
+// common p.  Per block of 128 threads: kNpBytes.
+constexpr int kNpBytes = (kPair + 1) * 128 * 2;
+
+struct LaneNp {
+  uint16_t *s;    // nullptr: no array (the interpreter stays in its basic mode)
+  uint32_t base;  // tid within the 128-thread block
+  __host__ __device__ __forceinline__ uint32_t get(int p) const {
+    return s[base + (static_cast<uint32_t>(p) << 7)];
+  }
+  __host__ __device__ __forceinline__ void set(int p, uint32_t v) const {
+    s[base + (static_cast<uint32_t>(p) << 7)] = static_cast<uint16_t>(v);
+  }
+};
+
 }  // namespace cubff

@@ -73,7 +73,7 @@ struct PipeQueue {
 // (grid-constant) parameter, so that a launch needs no host-to-device copy
 // and can be captured in a CUDA graph.  All soups have the queue's language;
 // the queue serves soups [first_soup, first_soup + n_soups) = all of them.
-constexpr int kMaxPipeSoups = 128;
+constexpr int kMaxPipeSoups = 64;
 struct PipeBatch {
   PipeSoup soups[kMaxPipeSoups];
   PipeQueue queue;

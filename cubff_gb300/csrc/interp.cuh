@@ -59,9 +59,11 @@ struct LaneMachine {
     if constexpr (L <= kBffSelfmove) m.begin(t, cmd_mask);
     else m.begin();
   }
+  // np: the BFF next-command array (fast mode), ignored by the other families.
   __host__ __device__ __forceinline__ bool step(const LaneBytes t, const LaneBytes stk,
+                                                const LaneNp np,
                                                 const uint8_t *__restrict__ optab) {
-    if constexpr (L <= kBffSelfmove) return m.step(t, stk, optab);
+    if constexpr (L <= kBffSelfmove) return m.step_lane(t, stk, np, optab);
     else if constexpr (LangTraits<L>::kForthFamily) return m.step(t, stk, optab);
     else return m.step(t, stk);
   }

@@ -138,7 +138,7 @@ __device__ __forceinline__ int soup_of_slot(const PipeSoup *soups, int lo, int h
 template <int L>
 __device__ __forceinline__ bool iterate(const PipeCtx &b, const PipeQueue &q, Lane &ln,
                                         LaneMachine<L> &m, const LaneBytes t, const LaneBytes stk,
-                                        const uint8_t *__restrict__ optab,
+                                        const LaneNp np, const uint8_t *__restrict__ optab,
                                         const uint8_t *__restrict__ cmdflag, uint32_t lane,
                                         uint32_t slot_ctr) {
   constexpr bool kBffFam = (L <= kBffSelfmove);
@@ -282,7 +282,7 @@ __device__ __forceinline__ bool iterate(const PipeCtx &b, const PipeQueue &q, La
     // Pairs that have run long are the ones later epochs wait on: give them
     // more steps per visit of the warp.
     const int steps = m.raw() > kLongRaw ? kStepsLong : kStepsPerVisit;
-    for (int r = 0; r < steps && !fin; r++) fin = m.step(t, stk, optab);
+    for (int r = 0; r < steps && !fin; r++) fin = m.step(t, stk, np, optab);
     if (fin) {
       const PipeSoup &sp = b.soups[ln.si];
       if (ln.dirty || (ln.evaluated && m.mods() != 0)) {
@@ -346,7 +346,8 @@ template <int L>
 __device__ __forceinline__ void serve(const PipeCtx &b, const PipeQueue &q,
                                       const uint8_t *__restrict__ optab,
                                       const uint8_t *__restrict__ cmdflag, const LaneBytes t,
-                                      const LaneBytes stk, uint32_t lane, uint32_t slot_ctr) {
+                                      const LaneBytes stk, const LaneNp np, uint32_t lane,
+                                      uint32_t slot_ctr) {
   Lane ln;
   ln.state = kIdle;
   ln.slot = ln.task = ln.e = ln.k = ln.p1 = ln.p2 = ln.qv = 0;
@@ -358,17 +359,35 @@ __device__ __forceinline__ void serve(const PipeCtx &b, const PipeQueue &q,
   ln.mm = make_uint4(0, 0, 0, 0);
   LaneMachine<L> m;
   while (true) {
-    const bool progressed = iterate<L>(b, q, ln, m, t, stk, optab, cmdflag, lane, slot_ctr);
+    const bool progressed = iterate<L>(b, q, ln, m, t, stk, np, optab, cmdflag, lane, slot_ctr);
     if (__all_sync(0xffffffffu, ln.state == kExhausted)) return;
     if (!__any_sync(0xffffffffu, progressed)) __nanosleep(200);
   }
 }
 
-// The persistent kernel of a pipelined launch over soups of language L.
+// Shared memory of a pipelined launch: the tape and second areas, the BFF
+// next-command arrays (BFF family only), the op and command tables, then the
+// soup descriptors.
 template <int L>
-__global__ void __launch_bounds__(kThreads, 4) pipeline_kernel(const __grid_constant__ PipeBatch pb) {
+__host__ __device__ constexpr size_t pipeline_np_bytes() {
+  return L <= kBffSelfmove ? size_t(kNpBytes) : 0;
+}
+
+template <int L>
+size_t pipeline_smem_bytes(int n_soups) {
+  return 2 * kGroups * kGroupBytes + pipeline_np_bytes<L>() + 512 +
+         size_t(n_soups) * sizeof(PipeSoup);
+}
+
+// The persistent kernel of a pipelined launch over soups of language L.  The
+// BFF family's larger shared-memory footprint allows 3 blocks per SM, the
+// others 4; the register budget follows.
+template <int L>
+__global__ void __launch_bounds__(kThreads, (L <= kBffSelfmove) ? 3 : 4)
+    pipeline_kernel(const __grid_constant__ PipeBatch pb) {
   extern __shared__ __align__(16) uint8_t smem[];
-  uint8_t *optab = smem + 2 * kGroups * kGroupBytes;
+  uint16_t *npa = reinterpret_cast<uint16_t *>(smem + 2 * kGroups * kGroupBytes);
+  uint8_t *optab = smem + 2 * kGroups * kGroupBytes + pipeline_np_bytes<L>();
   uint8_t *cmdflag = optab + 256;
   PipeSoup *soups = reinterpret_cast<PipeSoup *>(optab + 512);
   const uint32_t tid = threadIdx.x, lane = tid & 31;
@@ -388,20 +407,17 @@ __global__ void __launch_bounds__(kThreads, 4) pipeline_kernel(const __grid_cons
   const LaneBytes t{smem, lane_base(tid)};
   const LaneBytes stk{smem + kGroups * kGroupBytes, lane_base(tid)};
   const uint32_t warp = blockIdx.x * (kThreads / 32) + (tid >> 5);
+  const LaneNp np{L <= kBffSelfmove ? npa : nullptr, tid};
   const PipeCtx b{soups, pb.error};
   const PipeQueue q = pb.queue;
-  serve<L>(b, q, optab, cmdflag, t, stk, lane, warp % kCountSlots);
-}
-
-size_t pipeline_smem_bytes(int n_soups) {
-  return 2 * kGroups * kGroupBytes + 512 + size_t(n_soups) * sizeof(PipeSoup);
+  serve<L>(b, q, optab, cmdflag, t, stk, np, lane, warp % kCountSlots);
 }
 
 template <int L>
 int launch_pipeline_t(const PipeBatch &b, uint64_t total_pairs, uint32_t lanes_per_pair64,
                       int device, cudaStream_t stream) {
   static int sms_cache[64] = {0};
-  const size_t smem_max = pipeline_smem_bytes(kMaxPipeSoups);
+  const size_t smem_max = pipeline_smem_bytes<L>(kMaxPipeSoups);
   if (sms_cache[device & 63] == 0) {
     CUBFF_CUDA_TRY(cudaFuncSetAttribute(pipeline_kernel<L>,
                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -410,7 +426,7 @@ int launch_pipeline_t(const PipeBatch &b, uint64_t total_pairs, uint32_t lanes_p
     CUBFF_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
     sms_cache[device & 63] = sms;
   }
-  const size_t smem = pipeline_smem_bytes(b.n_soups);
+  const size_t smem = pipeline_smem_bytes<L>(b.n_soups);
   int per_sm = 0;
   CUBFF_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, pipeline_kernel<L>,
                                                                kThreads, smem));

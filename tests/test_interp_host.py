@@ -35,6 +35,9 @@ def host_lib():
     L = ctypes.CDLL(SO)
     L.host_evaluate.restype = ctypes.c_uint32
     L.host_evaluate.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]
+    L.host_evaluate_lane.restype = ctypes.c_uint32
+    L.host_evaluate_lane.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_uint32,
+                                     ctypes.c_void_p]
     return L
 
 
@@ -53,14 +56,25 @@ def dense_bytes(lang: str) -> np.ndarray:
     return np.frombuffer(b"[]+-.,<>{}\x00a", dtype=np.uint8)
 
 
+SWITCH_POINTS = (0, 1, 5, 1000)
+
+
 def check(L, lang, tape):
+    """The one-shot interpreter (basic mode) and the resumable lane machine
+    (BFF machines switching to fast mode after 0, 1, 5 or kFastAfter basic
+    steps) against the oracle."""
     a = tape.copy()
-    b = tape.copy()
     want_ops, want_raw = O.evaluate(lang, a)
+    b = tape.copy()
     raw = np.zeros(1, dtype=np.uint32)
     got_ops = L.host_evaluate(LANGUAGES.index(lang), b.ctypes.data, raw.ctypes.data)
     assert (got_ops, int(raw[0])) == (want_ops, want_raw), (lang, bytes(tape).hex())
     assert np.array_equal(a, b), (lang, bytes(tape).hex())
+    for sw in SWITCH_POINTS:
+        c = tape.copy()
+        got_ops = L.host_evaluate_lane(LANGUAGES.index(lang), c.ctypes.data, sw, raw.ctypes.data)
+        assert (got_ops, int(raw[0])) == (want_ops, want_raw), (lang, sw, bytes(tape).hex())
+        assert np.array_equal(a, c), (lang, sw, bytes(tape).hex())
 
 
 @pytest.mark.parametrize("lang", LANGUAGES)
@@ -110,3 +124,23 @@ def test_crafted_loops(host_lib, lang):
         tape2 = tape.copy()
         tape2[len(prog):] = 0x61
         check(host_lib, lang, tape2)
+
+
+@pytest.mark.parametrize("lang", ["bff_noheads", "bff"])
+def test_long_running_pairs_of_an_evolved_soup(host_lib, lang):
+    """The pairs of epoch 256 of an evolved soup (2^13 programs, seed 1) that
+    run longest: sweeping loops and counters that run to the step limit,
+    the work that the fast mode exists for."""
+    n = 1 << 13
+    soup = O.OracleSim(lang, n, 1, 1 << 18).run(lambda *a: False, 1, max_epochs=256)
+    perm = O.pairing_shuffle(1, 256, n)
+    progs = soup.reshape(n, 64)
+    tapes = np.concatenate([progs[perm[0::2]], progs[perm[1::2]]], axis=1)
+    raws = []
+    for k in range(n // 2):
+        _, r = O.evaluate(lang, tapes[k].copy())
+        raws.append(r)
+    order = np.argsort(raws)[::-1][:64]
+    assert raws[order[0]] == 8192
+    for k in order:
+        check(host_lib, lang, tapes[k].copy())
