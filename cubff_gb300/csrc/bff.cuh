@@ -26,14 +26,16 @@
 //    repetitions advance i by k*P, nskip by k times the segment's skips and
 //    the head by k times its shift (mod 128).
 //
-// Fast mode.  A pair that is still running after kFastAfter steps switches,
-// when the caller provides a next-command array (LaneNp), to a mode in which
-// one 16-bit entry per position gives the next command position >= p and its
-// op (entry = q << 4 | op, q = 128 when none): a step's fetch and no-op run
-// are one shared-memory load, issued one step ahead.  The bytes under the two
-// heads are cached in registers (v0, v1).  Writes that change a byte's op
-// rewrite the entries of the positions whose next command it is.  Both modes
-// share all other state, so the switch changes nothing in the results.
+// Two ways to step, with the same results:
+//  * basic mode (step_basic; the one-shot bff_eval of the per-epoch kernels):
+//    the next command comes from the command mask, its op from the table;
+//  * fast mode (step_lane; the lanes of the pipelined kernel, which provide
+//    a next-command array, LaneNp): one 16-bit entry per position gives the
+//    next command position >= p and its op (entry = q << 4 | op, q = 128 when
+//    none), so a step's fetch and no-op run are one shared-memory load,
+//    issued one step ahead.  The bytes under the two heads are cached in
+//    registers (v0, v1).  Writes that change a byte's op rewrite the entries
+//    of the positions whose next command it is.
 #pragma once
 
 #include "cycle.cuh"
@@ -43,13 +45,10 @@ namespace cubff {
 
 enum BffLogic { kLogicScan, kLogicJump8, kLogicSelfmove };
 
-constexpr uint32_t kFastAfter = 32;  // basic-mode steps before the switch
-
 template <bool kHeads, int kLogic, uint32_t kNullMask>
 struct BffMachine {
   int pc, h0, h1;
   uint32_t i, nskip, mods;
-  uint32_t nbasic;    // steps taken in basic mode
   bool fast;          // fast mode: np holds the next-command entries
   uint32_t v0, v1;    // fast mode: tape[h0], tape[h1]
   uint32_t nxt;       // fast mode: np entry of pc, loaded one step ahead
@@ -74,7 +73,6 @@ struct BffMachine {
       pc = 0;
     }
     i = nskip = mods = 0;
-    nbasic = 0;
     fast = false;
     v0 = v1 = nxt = 0;
     used0 = used1 = false;
@@ -313,20 +311,8 @@ struct BffMachine {
     return step_fast(t, snapa, np, optab);
   }
 
-  // One step: a run of no-ops (if any) and then one command.  Returns true
-  // when the program has ended; the op count is then i - nskip.  np may have
-  // no array (np.s == nullptr): the machine then stays in basic mode.
-  __host__ __device__ __forceinline__ bool step(const LaneBytes t, const LaneBytes snapa,
-                                                const LaneNp np,
-                                                const uint8_t *__restrict__ optab) {
-    if (fast) return step_fast(t, snapa, np, optab);
-    if (np.s && ++nbasic > kFastAfter) {
-      enter_fast(t, np, optab);
-      return step_fast(t, snapa, np, optab);
-    }
-    return step_basic(t, snapa, optab);
-  }
-
+  // Basic mode: a run of no-ops (if any) and then one command.  Returns true
+  // when the program has ended; the op count is then i - nskip.
   __host__ __device__ __forceinline__ bool step_basic(const LaneBytes t, const LaneBytes snapa,
                                                       const uint8_t *__restrict__ optab) {
     const int q = mask_next(cmd, pc);

@@ -51,12 +51,10 @@ extern "C" uint32_t host_evaluate(int lang, uint8_t *tape, uint32_t *raw) {
 
 namespace {
 
-// The resumable machine as the pipelined kernel runs it (LaneMachine<L>),
-// with a next-command array, switching BFF machines to fast mode after
-// switch_after basic steps.
+// The resumable machine as the pipelined kernel runs it (LaneMachine<L>,
+// BFF machines in fast mode with a next-command array).
 template <int L>
-uint32_t run_lane(uint8_t *buf, uint16_t *npbuf, const uint8_t *optab, uint32_t switch_after,
-                  uint32_t *raw) {
+uint32_t run_lane(uint8_t *buf, uint16_t *npbuf, const uint8_t *optab, uint32_t *raw) {
   const LaneBytes t{buf, 0};
   const LaneBytes stk{buf + kGroupBytes, 0};
   const LaneNp np{npbuf, 0};
@@ -64,8 +62,6 @@ uint32_t run_lane(uint8_t *buf, uint16_t *npbuf, const uint8_t *optab, uint32_t 
   Mask128 cmd{0, 0};
   for (int p = 0; p < kPair; p++) mask_assign(cmd, p, op_of(L, t.get(p)) < kNull);
   m.begin(t, cmd);
-  if constexpr (L <= kBffSelfmove)
-    m.m.nbasic = kFastAfter - (switch_after < kFastAfter ? switch_after : kFastAfter);
   while (!m.step(t, stk, np, optab)) {
   }
   *raw = m.raw();
@@ -74,8 +70,7 @@ uint32_t run_lane(uint8_t *buf, uint16_t *npbuf, const uint8_t *optab, uint32_t 
 
 }  // namespace
 
-extern "C" uint32_t host_evaluate_lane(int lang, uint8_t *tape, uint32_t switch_after,
-                                       uint32_t *raw) {
+extern "C" uint32_t host_evaluate_lane(int lang, uint8_t *tape, uint32_t *raw) {
   static thread_local uint8_t buf[2 * kGroupBytes];
   static thread_local uint16_t npbuf[kNpBytes / 2];
   uint8_t optab[256];
@@ -87,19 +82,19 @@ extern "C" uint32_t host_evaluate_lane(int lang, uint8_t *tape, uint32_t switch_
   for (int p = 0; p <= kPair; p++) npbuf[p << 7] = static_cast<uint16_t>(0xABCD + p);
   uint32_t ops = 0;
   switch (lang) {
-    case kBff: ops = run_lane<kBff>(buf, npbuf, optab, switch_after, raw); break;
-    case kBffNoheads: ops = run_lane<kBffNoheads>(buf, npbuf, optab, switch_after, raw); break;
-    case kBffNoheads4bit: ops = run_lane<kBffNoheads4bit>(buf, npbuf, optab, switch_after, raw); break;
-    case kBffPerm: ops = run_lane<kBffPerm>(buf, npbuf, optab, switch_after, raw); break;
-    case kBff8: ops = run_lane<kBff8>(buf, npbuf, optab, switch_after, raw); break;
-    case kBff8Noheads: ops = run_lane<kBff8Noheads>(buf, npbuf, optab, switch_after, raw); break;
-    case kBffSelfmove: ops = run_lane<kBffSelfmove>(buf, npbuf, optab, switch_after, raw); break;
-    case kForth: ops = run_lane<kForth>(buf, npbuf, optab, switch_after, raw); break;
-    case kForthcopy: ops = run_lane<kForthcopy>(buf, npbuf, optab, switch_after, raw); break;
-    case kForthtrivial: ops = run_lane<kForthtrivial>(buf, npbuf, optab, switch_after, raw); break;
-    case kForthtrivialReset: ops = run_lane<kForthtrivialReset>(buf, npbuf, optab, switch_after, raw); break;
-    case kSubleq: ops = run_lane<kSubleq>(buf, npbuf, optab, switch_after, raw); break;
-    case kRsubleq4: ops = run_lane<kRsubleq4>(buf, npbuf, optab, switch_after, raw); break;
+    case kBff: ops = run_lane<kBff>(buf, npbuf, optab, raw); break;
+    case kBffNoheads: ops = run_lane<kBffNoheads>(buf, npbuf, optab, raw); break;
+    case kBffNoheads4bit: ops = run_lane<kBffNoheads4bit>(buf, npbuf, optab, raw); break;
+    case kBffPerm: ops = run_lane<kBffPerm>(buf, npbuf, optab, raw); break;
+    case kBff8: ops = run_lane<kBff8>(buf, npbuf, optab, raw); break;
+    case kBff8Noheads: ops = run_lane<kBff8Noheads>(buf, npbuf, optab, raw); break;
+    case kBffSelfmove: ops = run_lane<kBffSelfmove>(buf, npbuf, optab, raw); break;
+    case kForth: ops = run_lane<kForth>(buf, npbuf, optab, raw); break;
+    case kForthcopy: ops = run_lane<kForthcopy>(buf, npbuf, optab, raw); break;
+    case kForthtrivial: ops = run_lane<kForthtrivial>(buf, npbuf, optab, raw); break;
+    case kForthtrivialReset: ops = run_lane<kForthtrivialReset>(buf, npbuf, optab, raw); break;
+    case kSubleq: ops = run_lane<kSubleq>(buf, npbuf, optab, raw); break;
+    case kRsubleq4: ops = run_lane<kRsubleq4>(buf, npbuf, optab, raw); break;
   }
   for (int p = 0; p < kPair; p++) tape[p] = buf[p << 7];
   return ops;
