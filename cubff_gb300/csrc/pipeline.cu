@@ -61,7 +61,7 @@ __global__ void mutation_mask_kernel(uint64_t s0, uint64_t e0, uint64_t npairs, 
 
 constexpr int kCountSlots = kPipeCountSlots;  // per-epoch counter slots (spread the atomics)
 constexpr int kStepsPerVisit = 8;
-constexpr int kStepsLong = 64;
+constexpr int kStepsLong = 256;
 constexpr uint32_t kLongRaw = 256;
 
 // Ready-queue dataflow over one or more soups.  A pair of epoch e+1 can run
