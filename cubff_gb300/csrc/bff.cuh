@@ -163,18 +163,51 @@ struct BffMachine {
 
   // Fast mode: builds the next-command entries and the bracket masks, loads
   // the head caches and the entry of pc.
+  //
+  // With bracket scanning (all variants but bff8), pc only ever continues
+  // after a command (at q + 1) or starts at the initial pc, so only the
+  // entries at q + 1 of commands q are kept (the initial fetch is computed
+  // here).  bff8's jumps (pc +- 8) land anywhere: it keeps every entry.
+  __host__ __device__ __forceinline__ uint32_t entry_at(const LaneBytes t,
+                                                        const uint8_t *__restrict__ optab,
+                                                        int q) const {
+    return q < kPair ? (uint32_t(q) << 4) | optab[t.get(q)] : uint32_t(kPair) << 4;
+  }
+
   __host__ __device__ __forceinline__ void enter_fast(const LaneBytes t, const LaneNp np,
                                                       const uint8_t *__restrict__ optab) {
-    if (!have_brk) build_brackets(t, optab);
-    uint32_t e = uint32_t(kPair) << 4;
-    np.set(kPair, e);
-    for (int p = kPair - 1; p >= 0; p--) {
-      if (mask_test(cmd, p)) e = (uint32_t(p) << 4) | optab[t.get(p)];
-      np.set(p, e);
+    if (kLogic == kLogicJump8) {
+      uint32_t e = uint32_t(kPair) << 4;
+      np.set(kPair, e);
+      for (int p = kPair - 1; p >= 0; p--) {
+        if (mask_test(cmd, p)) e = (uint32_t(p) << 4) | optab[t.get(p)];
+        np.set(p, e);
+      }
+      nxt = np.get(pc);
+    } else {
+      // Commands from the top down: np[q + 1] = entry of the next command
+      // after q; the bracket masks on the way.
+      opn = Mask128{0, 0};
+      cls = Mask128{0, 0};
+      uint32_t e = uint32_t(kPair) << 4;
+      for (int half = 1; half >= 0; half--) {
+        uint64_t w = half ? cmd.hi : cmd.lo;
+        while (w) {
+          const int b = 63 - clz64(w);
+          w &= ~(1ull << b);
+          const int q = 64 * half + b;
+          const uint32_t c = optab[t.get(q)];
+          np.set(q + 1, e);
+          if (c == kLoopStart) mask_assign(opn, q, true);
+          if (c == kLoopEnd) mask_assign(cls, q, true);
+          e = (uint32_t(q) << 4) | c;
+        }
+      }
+      have_brk = true;
+      nxt = entry_at(t, optab, mask_next(cmd, pc));
     }
     v0 = t.get(h0);
     v1 = t.get(h1);
-    nxt = np.get(pc);
     fast = true;
   }
 
@@ -199,9 +232,23 @@ struct BffMachine {
     mask_assign(cls, a, cn == kLoopEnd);
     if (!is && !was) return false;
     mask_assign(cmd, a, is);
-    const uint32_t ent = is ? ((uint32_t(a) << 4) | cn) : np.get(a + 1);
-    const int lo = mask_prev(cmd, a - 1) + 1;
-    for (int p = a; p >= lo; p--) np.set(p, ent);
+    if (kLogic == kLogicJump8) {
+      const uint32_t ent = is ? ((uint32_t(a) << 4) | cn) : np.get(a + 1);
+      const int lo = mask_prev(cmd, a - 1) + 1;
+      for (int p = a; p >= lo; p--) np.set(p, ent);
+    } else {
+      // The kept entries: a + 1 (when a becomes a command) and the one after
+      // the previous command, which now leads to a (or past it).
+      uint32_t ent;
+      if (is) {
+        ent = (uint32_t(a) << 4) | cn;
+        if (!was) np.set(a + 1, entry_at(t, optab, mask_next(cmd, a + 1)));
+      } else {
+        ent = np.get(a + 1);
+      }
+      const int pq = mask_prev(cmd, a - 1);
+      if (pq >= 0) np.set(pq + 1, ent);
+    }
     return true;
   }
 
