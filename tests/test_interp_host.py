@@ -120,11 +120,11 @@ def test_crafted_loops(host_lib, lang):
         check(host_lib, lang, tape2)
 
 
-@pytest.mark.parametrize("lang", ["bff_noheads", "bff"])
+@pytest.mark.parametrize("lang", ["bff_noheads", "bff", "forth"])
 def test_long_running_pairs_of_an_evolved_soup(host_lib, lang):
     """The pairs of epoch 256 of an evolved soup (2^13 programs, seed 1) that
     run longest: sweeping loops and counters that run to the step limit,
-    the work that the fast mode exists for."""
+    where the interpreters' per-step paths matter most."""
     n = 1 << 13
     soup = O.OracleSim(lang, n, 1, 1 << 18).run(lambda *a: False, 1, max_epochs=256)
     perm = O.pairing_shuffle(1, 256, n)
