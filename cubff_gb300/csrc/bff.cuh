@@ -52,6 +52,13 @@ struct BffMachine {
   bool fast;          // fast mode: np holds the next-command entries
   uint32_t v0, v1;    // fast mode: tape[h0], tape[h1]
   uint32_t nxt;       // fast mode: np entry of pc, loaded one step ahead
+  // Fast mode, loop replay: a loop [ ... ] whose body has no brackets and at
+  // most 16 commands runs from its op list, one command per step, the no-op
+  // runs and the step count of an iteration accounted at its ']'.
+  // rpk = S | E << 8 | m << 16 | j << 24 ('[' at S, ']' at E, m body
+  // commands, j of them done in this iteration); 0 = not replaying.
+  uint32_t rpk;
+  uint64_t rcls, rc;  // body ops, 4 bits each, first in the low bits; rc = the rest
   bool have_brk;
   bool used0, used1;  // heads used as addresses since the snapshot
   Mask128 cmd, opn, cls;
@@ -75,6 +82,8 @@ struct BffMachine {
     i = nskip = mods = 0;
     fast = false;
     v0 = v1 = nxt = 0;
+    rpk = 0;
+    rcls = rc = 0;
     used0 = used1 = false;
     touched = Mask128{0, 0};
     s_pc = -1;
@@ -213,12 +222,13 @@ struct BffMachine {
 
   // write() for fast mode: also rewrites the next-command entries of the
   // positions after the previous command up to a when a's op changes.
-  // Returns true when entries changed (the prefetched entry may be stale).
-  __host__ __device__ __forceinline__ bool write_fast(const LaneBytes t, const LaneBytes snapa,
+  // Returns 0 when no entry changed, else 1 + (a was a command): the
+  // prefetched entry may be stale.
+  __host__ __device__ __forceinline__ int write_fast(const LaneBytes t, const LaneBytes snapa,
                                                       const LaneNp np,
                                                       const uint8_t *__restrict__ optab, int a,
                                                       uint32_t o, uint32_t v) {
-    if (v == o) return false;
+    if (v == o) return 0;
     t.set(a, v);
     mods++;
     if (!mask_test(touched, a)) {
@@ -226,11 +236,11 @@ struct BffMachine {
       snapa.set(a, o);
     }
     const uint32_t co = optab[o], cn = optab[v];
-    if (co == cn) return false;
+    if (co == cn) return 0;
     const bool is = cn < kNull, was = co < kNull;
     mask_assign(opn, a, cn == kLoopStart);
     mask_assign(cls, a, cn == kLoopEnd);
-    if (!is && !was) return false;
+    if (!is && !was) return 0;
     mask_assign(cmd, a, is);
     if (kLogic == kLogicJump8) {
       const uint32_t ent = is ? ((uint32_t(a) << 4) | cn) : np.get(a + 1);
@@ -249,7 +259,7 @@ struct BffMachine {
       const int pq = mask_prev(cmd, a - 1);
       if (pq >= 0) np.set(pq + 1, ent);
     }
-    return true;
+    return 1 + was;
   }
 
   __host__ __device__ __forceinline__ bool step_fast(const LaneBytes t, const LaneBytes snapa,
@@ -273,6 +283,7 @@ struct BffMachine {
     int npc = pc + 1;
     nxt = np.get(npc);  // npc <= kPair: the sentinel entry exists
     bool back = false;
+    int pe = 0;  // a ']' taken backwards: its position
     if (c >= kDec0) {
       if (c <= kInc0) {
         h0 = (h0 + (c == kInc0 ? 1 : -1)) & (kPair - 1);
@@ -316,6 +327,7 @@ struct BffMachine {
       }
     } else {
       used0 = true;
+      pe = pc;
       if ((v0 & kNullMask) != 0) {
         back = true;
         if (kLogic == kLogicJump8) {
@@ -345,7 +357,119 @@ struct BffMachine {
       if (i >= kStepLimit) return true;
       if (h0 != g0) v0 = t.get(h0);
       if (h1 != g1) v1 = t.get(h1);
+      if (kLogic != kLogicJump8) enter_replay(np, pc - 1, pe);
     }
+    return false;
+  }
+
+  // Bits a..b (inclusive) of one 64-bit mask word (none when a > b).
+  __host__ __device__ __forceinline__ static uint64_t word_bits(int a, int b) {
+    return a > b ? 0ull : (~0ull >> (63 - b)) & (~0ull << a);
+  }
+  // Positions strictly between s and e (0 <= s < e <= 127) of mask m.
+  __host__ __device__ __forceinline__ static Mask128 between(const Mask128 &m, int s, int e) {
+    const int lo_end = e - 1 < 63 ? e - 1 : 63;
+    const int hi_start = s + 1 > 64 ? s + 1 : 64;
+    return Mask128{m.lo & word_bits(s + 1, lo_end), m.hi & word_bits(hi_start - 64, e - 1 - 64)};
+  }
+
+  // After the ']' at e jumped back to the '[' at s: replay the loop when its
+  // body has no brackets and at most 16 commands (their ops come from the
+  // next-command entries, which chain from s through the body to e).
+  __host__ __device__ __forceinline__ void enter_replay(const LaneNp np, int s, int e) {
+    const Mask128 body = between(cmd, s, e);
+    const Mask128 brk = between(Mask128{opn.lo | cls.lo, opn.hi | cls.hi}, s, e);
+    if (brk.lo | brk.hi) return;
+    const int m = popc64(body.lo) + popc64(body.hi);
+    if (m > 16) return;
+    uint64_t ops = 0;
+    int q = s;
+    for (int k = 0; k < m; k++) {
+      const uint32_t en = np.get(q + 1);
+      q = static_cast<int>(en >> 4);
+      ops |= static_cast<uint64_t>(en & 15) << (4 * k);
+    }
+    rcls = rc = ops;
+    rpk = static_cast<uint32_t>(s) | (static_cast<uint32_t>(e) << 8) |
+          (static_cast<uint32_t>(m) << 16);
+  }
+
+  // One step of a replayed loop: the next body command, or the closing ']'.
+  __host__ __device__ __forceinline__ bool step_replay(const LaneBytes t, const LaneBytes snapa,
+                                                       const LaneNp np,
+                                                       const uint8_t *__restrict__ optab) {
+    const int s = rpk & 0xFF, e = (rpk >> 8) & 0xFF, m = (rpk >> 16) & 0xFF, j = rpk >> 24;
+    const uint32_t len = static_cast<uint32_t>(e - s);  // raw steps of an iteration
+    if (j == 0 && i + len > kStepLimit) {
+      // Not a whole iteration left: continue step by step (no step taken here).
+      rpk = 0;
+      pc = s + 1;
+      nxt = np.get(pc);
+      return false;
+    }
+    if (j < m) {
+      const uint32_t c = rc & 15;
+      rc >>= 4;
+      rpk += 1u << 24;
+      if (c >= kDec0) {
+        if (c <= kInc0) {
+          h0 = (h0 + (c == kInc0 ? 1 : -1)) & (kPair - 1);
+          v0 = t.get(h0);
+        } else {
+          h1 = (h1 + (c == kInc1 ? 1 : -1)) & (kPair - 1);
+          v1 = t.get(h1);
+        }
+      } else {
+        used0 = true;
+        const bool to1 = c == kCopy01;
+        if (c >= kCopy01) used1 = true;
+        const int a = to1 ? h1 : h0;
+        const uint32_t o = to1 ? v1 : v0;
+        const uint32_t v = (c == kPlus ? v0 + 1 : c == kMinus ? v0 - 1 : to1 ? v0 : v1) & 0xFF;
+        if (to1) v1 = v; else v0 = v;
+        if (h0 == h1) v0 = v1 = v;
+        const int w = write_fast(t, snapa, np, optab, a, o, v);
+        if (kLogic == kLogicSelfmove && c == kCopy10) {
+          h1 = (h1 + 1) & (kPair - 1);
+          v1 = t.get(h1);
+        }
+        if (w && a >= s && a <= e) {
+          // The loop changed its own code: stop replaying after this command.
+          // Body command j sits at the (j+1)-th position of the body as it
+          // was (a's bit as before the write).
+          Mask128 body = between(cmd, s, e);
+          if (a > s && a < e) mask_assign(body, a, w == 2);
+          int p = s;
+          for (int k = 0; k <= j; k++) p = mask_next(body, p + 1);
+          i += static_cast<uint32_t>(p - s);
+          nskip += static_cast<uint32_t>(p - s - (j + 1));
+          rpk = 0;
+          pc = p + 1;
+          nxt = np.get(pc);
+        }
+      }
+      return false;
+    }
+    // The ']' at e: the iteration's raw steps and no-ops, then its test.
+    i += len;
+    nskip += len - 1 - m;
+    used0 = true;
+    if ((v0 & kNullMask) == 0) {
+      rpk = 0;
+      pc = e + 1;
+      if (pc >= kPair || i >= kStepLimit) return true;
+      nxt = np.get(pc);
+      return false;
+    }
+    pc = s + 1;
+    if (i >= kStepLimit) return true;
+    const int g0 = h0, g1 = h1;
+    visit(t, snapa);
+    if (i >= kStepLimit) return true;
+    if (h0 != g0) v0 = t.get(h0);
+    if (h1 != g1) v1 = t.get(h1);
+    rc = rcls;
+    rpk &= 0x00FFFFFFu;
     return false;
   }
 
@@ -355,6 +479,7 @@ struct BffMachine {
                                                      const LaneNp np,
                                                      const uint8_t *__restrict__ optab) {
     if (!fast) enter_fast(t, np, optab);
+    if (rpk) return step_replay(t, snapa, np, optab);
     return step_fast(t, snapa, np, optab);
   }
 

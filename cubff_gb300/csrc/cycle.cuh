@@ -28,6 +28,14 @@ __host__ __device__ __forceinline__ int ffs64(uint64_t x) {
 #endif
 }
 
+__host__ __device__ __forceinline__ int popc64(uint64_t x) {
+#ifdef __CUDA_ARCH__
+  return __popcll(static_cast<long long>(x));
+#else
+  return __builtin_popcountll(x);
+#endif
+}
+
 // Count of leading zeros of a non-zero x.
 __host__ __device__ __forceinline__ int clz64(uint64_t x) {
 #ifdef __CUDA_ARCH__

@@ -93,6 +93,9 @@ CRAFTED = {
                     # head-1 drift loops (h1 moves, never used as an address)
                     b"+[}]", b"+[{{}" + b"q" * 30 + b"]", b"+[}}}" + b"q" * 60 + b"]",
                     b"+[}.]", b"+[},]", b"+[}" + b"q" * 50 + b"{{]",
+                    # loops that run into their own code (replay stops on the change)
+                    b"+[>+]", b"+[>>+]", b"+[<+]", b"+[<-]", b"+[>.]", b"+[}>,]", b"+[>+<.>]",
+                    b"+[" + b"q" * 5 + b">+" + b"q" * 7 + b"]", b"-[>-]" + b"+" * 20,
                     # a tape that ran 6241 loop iterations of an h1-drift loop
                     bytes.fromhex(
                         "515b7d7b7b7d7d7b807d7d197b7d7d7b7b7d7d7b7b7d7d7b7b7dba7b7b7d7d7b7b7d7d"
