@@ -52,13 +52,16 @@ struct BffMachine {
   bool fast;          // fast mode: np holds the next-command entries
   uint32_t v0, v1;    // fast mode: tape[h0], tape[h1]
   uint32_t nxt;       // fast mode: np entry of pc, loaded one step ahead
-  // Fast mode, loop replay: a loop [ ... ] whose body has no brackets and at
-  // most 16 commands runs from its op list, one command per step, the no-op
-  // runs and the step count of an iteration accounted at its ']'.
+  // Fast mode, loop replay: a loop [ ... ] whose body has no brackets runs
+  // from its op list, one op per step, the no-op runs and the step count of
+  // an iteration accounted at its ']'.  Runs of one head move merge into one
+  // op (h +- r), and so do runs of '.' or ',' (a repeat copies a value onto
+  // itself); at most 8 ops of at most 16 commands each.
   // rpk = S | E << 8 | m << 16 | j << 24 ('[' at S, ']' at E, m body
-  // commands, j of them done in this iteration); 0 = not replaying.
+  // commands, j ops done in this iteration); 0 = not replaying.
   uint32_t rpk;
-  uint64_t rcls, rc;  // body ops, 4 bits each, first in the low bits; rc = the rest
+  uint64_t rcls, rc;  // ops: 8 bits each (op | (count - 1) << 4), first in the low
+                      // bits; rc = the rest of this iteration (0 = only the ']')
   bool have_brk;
   bool used0, used1;  // heads used as addresses since the snapshot
   Mask128 cmd, opn, cls;
@@ -373,21 +376,38 @@ struct BffMachine {
     return Mask128{m.lo & word_bits(s + 1, lo_end), m.hi & word_bits(hi_start - 64, e - 1 - 64)};
   }
 
+  // Ops that a run of may merge into one replay op.
+  __host__ __device__ __forceinline__ static bool mergeable(uint32_t c) {
+    return c >= kDec0 || (kLogic != kLogicSelfmove && (c == kCopy01 || c == kCopy10));
+  }
+
   // After the ']' at e jumped back to the '[' at s: replay the loop when its
-  // body has no brackets and at most 16 commands (their ops come from the
-  // next-command entries, which chain from s through the body to e).
+  // body has no brackets and merges into at most 8 ops (the body's ops come
+  // from the next-command entries, which chain from s through the body to e).
   __host__ __device__ __forceinline__ void enter_replay(const LaneNp np, int s, int e) {
     const Mask128 body = between(cmd, s, e);
     const Mask128 brk = between(Mask128{opn.lo | cls.lo, opn.hi | cls.hi}, s, e);
     if (brk.lo | brk.hi) return;
     const int m = popc64(body.lo) + popc64(body.hi);
-    if (m > 16) return;
     uint64_t ops = 0;
+    int n = 0;             // ops so far
+    uint32_t last = 16;    // op of the current run (16 = none)
+    uint32_t cnt = 0;
     int q = s;
     for (int k = 0; k < m; k++) {
       const uint32_t en = np.get(q + 1);
       q = static_cast<int>(en >> 4);
-      ops |= static_cast<uint64_t>(en & 15) << (4 * k);
+      const uint32_t c = en & 15;
+      if (c == last && mergeable(c) && cnt < 16) {
+        cnt++;
+        ops += 1ull << (8 * (n - 1) + 4);
+      } else {
+        if (n == 8) return;
+        ops |= static_cast<uint64_t>(c) << (8 * n);
+        n++;
+        last = c;
+        cnt = 1;
+      }
     }
     rcls = rc = ops;
     rpk = static_cast<uint32_t>(s) | (static_cast<uint32_t>(e) << 8) |
@@ -407,16 +427,17 @@ struct BffMachine {
       nxt = np.get(pc);
       return false;
     }
-    if (j < m) {
+    if (rc != 0) {
       const uint32_t c = rc & 15;
-      rc >>= 4;
+      const int r = static_cast<int>((rc >> 4) & 15) + 1;  // commands merged into this op
+      rc >>= 8;
       rpk += 1u << 24;
       if (c >= kDec0) {
         if (c <= kInc0) {
-          h0 = (h0 + (c == kInc0 ? 1 : -1)) & (kPair - 1);
+          h0 = (h0 + (c == kInc0 ? r : -r)) & (kPair - 1);
           v0 = t.get(h0);
         } else {
-          h1 = (h1 + (c == kInc1 ? 1 : -1)) & (kPair - 1);
+          h1 = (h1 + (c == kInc1 ? r : -r)) & (kPair - 1);
           v1 = t.get(h1);
         }
       } else {
@@ -434,15 +455,18 @@ struct BffMachine {
           v1 = t.get(h1);
         }
         if (w && a >= s && a <= e) {
-          // The loop changed its own code: stop replaying after this command.
-          // Body command j sits at the (j+1)-th position of the body as it
-          // was (a's bit as before the write).
+          // The loop changed its own code: stop replaying after this command
+          // (the first of its op; a repeat writes nothing).  It is body
+          // command k = the commands of the ops before it, at the (k+1)-th
+          // position of the body as it was (a's bit as before the write).
+          int k = 0;
+          for (int o2 = 0; o2 < j; o2++) k += static_cast<int>((rcls >> (8 * o2 + 4)) & 15) + 1;
           Mask128 body = between(cmd, s, e);
           if (a > s && a < e) mask_assign(body, a, w == 2);
           int p = s;
-          for (int k = 0; k <= j; k++) p = mask_next(body, p + 1);
+          for (int k2 = 0; k2 <= k; k2++) p = mask_next(body, p + 1);
           i += static_cast<uint32_t>(p - s);
-          nskip += static_cast<uint32_t>(p - s - (j + 1));
+          nskip += static_cast<uint32_t>(p - s - (k + 1));
           rpk = 0;
           pc = p + 1;
           nxt = np.get(pc);

@@ -96,6 +96,9 @@ CRAFTED = {
                     # loops that run into their own code (replay stops on the change)
                     b"+[>+]", b"+[>>+]", b"+[<+]", b"+[<-]", b"+[>.]", b"+[}>,]", b"+[>+<.>]",
                     b"+[" + b"q" * 5 + b">+" + b"q" * 7 + b"]", b"-[>-]" + b"+" * 20,
+                    # runs that replay merges (head moves, repeated copies)
+                    b"+[}" + b"," * 12 + b"q.q]", b"+[>>>>+]", b"+[<<<<<<<<<-]", b"+[}}}.,,,,]",
+                    b"+[" + b">" * 20 + b"+" + b"<" * 19 + b"]", b"+[{{{{" + b"." * 17 + b"]",
                     # a tape that ran 6241 loop iterations of an h1-drift loop
                     bytes.fromhex(
                         "515b7d7b7b7d7d7b807d7d197b7d7d7b7b7d7d7b7b7d7d7b7b7dba7b7b7d7d7b7b7d7d"
