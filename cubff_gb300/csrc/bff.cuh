@@ -57,8 +57,9 @@ struct BffMachine {
   // an iteration accounted at its ']'.  Runs of one head move merge into one
   // op (h +- r), and so do runs of '.' or ',' (a repeat copies a value onto
   // itself); at most 8 ops of at most 16 commands each.
-  // rpk = S | E << 8 | m << 16 | j << 24 ('[' at S, ']' at E, m body
-  // commands, j ops done in this iteration); 0 = not replaying.
+  // rpk = S | E << 8 | m << 16 | j << 24 ('[' at S, ']' at E, m < 128 body
+  // commands, j ops done in this iteration), plus kScanLoop when the body
+  // only moves heads; 0 = not replaying.
   uint32_t rpk;
   uint64_t rcls, rc;  // ops: 8 bits each (op | (count - 1) << 4), first in the low
                       // bits; rc = the rest of this iteration (0 = only the ']')
@@ -376,6 +377,8 @@ struct BffMachine {
     return Mask128{m.lo & word_bits(s + 1, lo_end), m.hi & word_bits(hi_start - 64, e - 1 - 64)};
   }
 
+  static constexpr uint32_t kScanLoop = 1u << 23;
+
   // Ops that a run of may merge into one replay op.
   __host__ __device__ __forceinline__ static bool mergeable(uint32_t c) {
     return c >= kDec0 || (kLogic != kLogicSelfmove && (c == kCopy01 || c == kCopy10));
@@ -409,16 +412,68 @@ struct BffMachine {
         cnt = 1;
       }
     }
+    bool moves_only = true;
+    for (int o2 = 0; o2 < n; o2++) moves_only &= ((ops >> (8 * o2)) & 15) >= kDec0;
     rcls = rc = ops;
     rpk = static_cast<uint32_t>(s) | (static_cast<uint32_t>(e) << 8) |
-          (static_cast<uint32_t>(m) << 16);
+          (static_cast<uint32_t>(m) << 16) | (moves_only ? kScanLoop : 0u);
+  }
+
+  // A loop whose body only moves heads changes no byte, so its iterations
+  // differ only in the heads: each moves h0 by d0 and h1 by d1, and the ']'
+  // tests the byte under the new h0.  The iterations until that byte is a
+  // zero (all of them the step limit allows, when no position reachable by
+  // h0 holds one) are taken at once.  Returns 1 when the program ended, 0
+  // when the loop was taken over, -1 when it does not apply (d0 = 0 mod 128:
+  // the test never changes).
+  __host__ __device__ __forceinline__ int scan_loop(const LaneBytes t, const LaneNp np, int s,
+                                                    int e, int m, uint32_t len) {
+    int d0 = 0, d1 = 0;
+    for (uint64_t w = rcls; w; w >>= 8) {
+      const uint32_t c = w & 15;
+      const int r = static_cast<int>((w >> 4) & 15) + 1;
+      if (c == kInc0) d0 += r;
+      else if (c == kDec0) d0 -= r;
+      else if (c == kInc1) d1 += r;
+      else d1 -= r;
+    }
+    if ((d0 & (kPair - 1)) == 0) return -1;
+    const uint32_t lim = (kStepLimit - i) / len;  // whole iterations left, >= 1
+    const uint32_t kmax = lim < kPair ? lim : kPair;
+    uint32_t k = 1;
+    bool found = false;
+    for (; k <= kmax; k++) {
+      if ((t.get((h0 + static_cast<int>(k) * d0) & (kPair - 1)) & kNullMask) == 0) {
+        found = true;
+        break;
+      }
+    }
+    // No zero among the positions h0 reaches (all within kPair iterations):
+    // the loop runs until the step limit.
+    if (!found) k = lim;
+    h0 = (h0 + static_cast<int>(k) * d0) & (kPair - 1);
+    h1 = (h1 + static_cast<int>(k) * d1) & (kPair - 1);
+    v0 = t.get(h0);
+    v1 = t.get(h1);
+    i += k * len;
+    nskip += k * (len - 1 - static_cast<uint32_t>(m));
+    used0 = true;
+    if (found) {  // the k-th ']' falls through
+      rpk = 0;
+      pc = e + 1;
+      if (pc >= kPair || i >= kStepLimit) return 1;
+      nxt = np.get(pc);
+      return 0;
+    }
+    pc = s + 1;
+    return i >= kStepLimit ? 1 : 0;
   }
 
   // One step of a replayed loop: the next body command, or the closing ']'.
   __host__ __device__ __forceinline__ bool step_replay(const LaneBytes t, const LaneBytes snapa,
                                                        const LaneNp np,
                                                        const uint8_t *__restrict__ optab) {
-    const int s = rpk & 0xFF, e = (rpk >> 8) & 0xFF, m = (rpk >> 16) & 0xFF, j = rpk >> 24;
+    const int s = rpk & 0xFF, e = (rpk >> 8) & 0xFF, m = (rpk >> 16) & 0x7F, j = rpk >> 24;
     const uint32_t len = static_cast<uint32_t>(e - s);  // raw steps of an iteration
     if (j == 0 && i + len > kStepLimit) {
       // Not a whole iteration left: continue step by step (no step taken here).
@@ -426,6 +481,10 @@ struct BffMachine {
       pc = s + 1;
       nxt = np.get(pc);
       return false;
+    }
+    if (j == 0 && (rpk & kScanLoop)) {
+      const int r = scan_loop(t, np, s, e, m, len);
+      if (r >= 0) return r == 1;
     }
     if (rc != 0) {
       const uint32_t c = rc & 15;
