@@ -53,16 +53,14 @@ struct BffMachine {
   uint32_t v0, v1;    // fast mode: tape[h0], tape[h1]
   uint32_t nxt;       // fast mode: np entry of pc, loaded one step ahead
   // Fast mode, loop replay: a loop [ ... ] whose body has no brackets runs
-  // from its op list, one op per step, the no-op runs and the step count of
-  // an iteration accounted at its ']'.  Runs of one head move merge into one
+  // from its op list, one iteration per step, the no-op runs and the step
+  // count of an iteration accounted at its ']'.  Runs of one head move merge into one
   // op (h +- r), and so do runs of '.' or ',' (a repeat copies a value onto
   // itself); at most 8 ops of at most 16 commands each.
-  // rpk = S | E << 8 | m << 16 | j << 24 ('[' at S, ']' at E, m < 128 body
-  // commands, j ops done in this iteration), plus kScanLoop when the body
-  // only moves heads; 0 = not replaying.
+  // rpk = S | E << 8 | m << 16 ('[' at S, ']' at E, m < 128 body commands),
+  // plus kScanLoop when the body only moves heads; 0 = not replaying.
   uint32_t rpk;
-  uint64_t rcls, rc;  // ops: 8 bits each (op | (count - 1) << 4), first in the low
-                      // bits; rc = the rest of this iteration (0 = only the ']')
+  uint64_t rcls;  // ops: 8 bits each (op | (count - 1) << 4), first in the low bits
   bool have_brk;
   bool used0, used1;  // heads used as addresses since the snapshot
   Mask128 cmd, opn, cls;
@@ -87,7 +85,7 @@ struct BffMachine {
     fast = false;
     v0 = v1 = nxt = 0;
     rpk = 0;
-    rcls = rc = 0;
+    rcls = 0;
     used0 = used1 = false;
     touched = Mask128{0, 0};
     s_pc = -1;
@@ -414,7 +412,7 @@ struct BffMachine {
     }
     bool moves_only = true;
     for (int o2 = 0; o2 < n; o2++) moves_only &= ((ops >> (8 * o2)) & 15) >= kDec0;
-    rcls = rc = ops;
+    rcls = ops;
     rpk = static_cast<uint32_t>(s) | (static_cast<uint32_t>(e) << 8) |
           (static_cast<uint32_t>(m) << 16) | (moves_only ? kScanLoop : 0u);
   }
@@ -473,24 +471,24 @@ struct BffMachine {
   __host__ __device__ __forceinline__ bool step_replay(const LaneBytes t, const LaneBytes snapa,
                                                        const LaneNp np,
                                                        const uint8_t *__restrict__ optab) {
-    const int s = rpk & 0xFF, e = (rpk >> 8) & 0xFF, m = (rpk >> 16) & 0x7F, j = rpk >> 24;
+    const int s = rpk & 0xFF, e = (rpk >> 8) & 0xFF, m = (rpk >> 16) & 0x7F;
     const uint32_t len = static_cast<uint32_t>(e - s);  // raw steps of an iteration
-    if (j == 0 && i + len > kStepLimit) {
+    if (i + len > kStepLimit) {
       // Not a whole iteration left: continue step by step (no step taken here).
       rpk = 0;
       pc = s + 1;
       nxt = np.get(pc);
       return false;
     }
-    if (j == 0 && (rpk & kScanLoop)) {
+    if (rpk & kScanLoop) {
       const int r = scan_loop(t, np, s, e, m, len);
       if (r >= 0) return r == 1;
     }
-    if (rc != 0) {
-      const uint32_t c = rc & 15;
-      const int r = static_cast<int>((rc >> 4) & 15) + 1;  // commands merged into this op
-      rc >>= 8;
-      rpk += 1u << 24;
+    // The body's ops.
+    int j = 0;
+    for (uint64_t ops = rcls; ops != 0; ops >>= 8, j++) {
+      const uint32_t c = ops & 15;
+      const int r = static_cast<int>((ops >> 4) & 15) + 1;  // commands merged into this op
       if (c >= kDec0) {
         if (c <= kInc0) {
           h0 = (h0 + (c == kInc0 ? r : -r)) & (kPair - 1);
@@ -499,39 +497,39 @@ struct BffMachine {
           h1 = (h1 + (c == kInc1 ? r : -r)) & (kPair - 1);
           v1 = t.get(h1);
         }
-      } else {
-        used0 = true;
-        const bool to1 = c == kCopy01;
-        if (c >= kCopy01) used1 = true;
-        const int a = to1 ? h1 : h0;
-        const uint32_t o = to1 ? v1 : v0;
-        const uint32_t v = (c == kPlus ? v0 + 1 : c == kMinus ? v0 - 1 : to1 ? v0 : v1) & 0xFF;
-        if (to1) v1 = v; else v0 = v;
-        if (h0 == h1) v0 = v1 = v;
-        const int w = write_fast(t, snapa, np, optab, a, o, v);
-        if (kLogic == kLogicSelfmove && c == kCopy10) {
-          h1 = (h1 + 1) & (kPair - 1);
-          v1 = t.get(h1);
-        }
-        if (w && a >= s && a <= e) {
-          // The loop changed its own code: stop replaying after this command
-          // (the first of its op; a repeat writes nothing).  It is body
-          // command k = the commands of the ops before it, at the (k+1)-th
-          // position of the body as it was (a's bit as before the write).
-          int k = 0;
-          for (int o2 = 0; o2 < j; o2++) k += static_cast<int>((rcls >> (8 * o2 + 4)) & 15) + 1;
-          Mask128 body = between(cmd, s, e);
-          if (a > s && a < e) mask_assign(body, a, w == 2);
-          int p = s;
-          for (int k2 = 0; k2 <= k; k2++) p = mask_next(body, p + 1);
-          i += static_cast<uint32_t>(p - s);
-          nskip += static_cast<uint32_t>(p - s - (k + 1));
-          rpk = 0;
-          pc = p + 1;
-          nxt = np.get(pc);
-        }
+        continue;
       }
-      return false;
+      used0 = true;
+      const bool to1 = c == kCopy01;
+      if (c >= kCopy01) used1 = true;
+      const int a = to1 ? h1 : h0;
+      const uint32_t o = to1 ? v1 : v0;
+      const uint32_t v = (c == kPlus ? v0 + 1 : c == kMinus ? v0 - 1 : to1 ? v0 : v1) & 0xFF;
+      if (to1) v1 = v; else v0 = v;
+      if (h0 == h1) v0 = v1 = v;
+      const int w = write_fast(t, snapa, np, optab, a, o, v);
+      if (kLogic == kLogicSelfmove && c == kCopy10) {
+        h1 = (h1 + 1) & (kPair - 1);
+        v1 = t.get(h1);
+      }
+      if (w && a >= s && a <= e) {
+        // The loop changed its own code: stop replaying after this command
+        // (the first of its op; a repeat writes nothing).  It is body
+        // command k = the commands of the ops before it, at the (k+1)-th
+        // position of the body as it was (a's bit as before the write).
+        int k = 0;
+        for (int o2 = 0; o2 < j; o2++) k += static_cast<int>((rcls >> (8 * o2 + 4)) & 15) + 1;
+        Mask128 body = between(cmd, s, e);
+        if (a > s && a < e) mask_assign(body, a, w == 2);
+        int p = s;
+        for (int k2 = 0; k2 <= k; k2++) p = mask_next(body, p + 1);
+        i += static_cast<uint32_t>(p - s);
+        nskip += static_cast<uint32_t>(p - s - (k + 1));
+        rpk = 0;
+        pc = p + 1;
+        nxt = np.get(pc);
+        return false;
+      }
     }
     // The ']' at e: the iteration's raw steps and no-ops, then its test.
     i += len;
@@ -551,8 +549,6 @@ struct BffMachine {
     if (i >= kStepLimit) return true;
     if (h0 != g0) v0 = t.get(h0);
     if (h1 != g1) v1 = t.get(h1);
-    rc = rcls;
-    rpk &= 0x00FFFFFFu;
     return false;
   }
 
