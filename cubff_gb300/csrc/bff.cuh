@@ -376,10 +376,15 @@ struct BffMachine {
   }
 
   static constexpr uint32_t kScanLoop = 1u << 23;
+  static constexpr uint32_t kCountLoop = 1u << 24;
 
-  // Ops that a run of may merge into one replay op.
+  // Ops that a run of may merge into one replay op: head moves, copies (a
+  // repeat copies a value onto itself) and '+' / '-' (a run adds its length
+  // to one byte; it runs merged only while that byte is outside the loop's
+  // code, so no op of the loop changes on the way).
   __host__ __device__ __forceinline__ static bool mergeable(uint32_t c) {
-    return c >= kDec0 || (kLogic != kLogicSelfmove && (c == kCopy01 || c == kCopy10));
+    return c >= kDec0 || c == kPlus || c == kMinus ||
+           (kLogic != kLogicSelfmove && (c == kCopy01 || c == kCopy10));
   }
 
   // After the ']' at e jumped back to the '[' at s: replay the loop when its
@@ -412,9 +417,59 @@ struct BffMachine {
     }
     bool moves_only = true;
     for (int o2 = 0; o2 < n; o2++) moves_only &= ((ops >> (8 * o2)) & 15) >= kDec0;
+    const bool counter = n == 1 && ((ops & 15) == kPlus || (ops & 15) == kMinus);
     rcls = ops;
     rpk = static_cast<uint32_t>(s) | (static_cast<uint32_t>(e) << 8) |
-          (static_cast<uint32_t>(m) << 16) | (moves_only ? kScanLoop : 0u);
+          (static_cast<uint32_t>(m) << 16) | (moves_only ? kScanLoop : 0u) |
+          (counter ? kCountLoop : 0u);
+  }
+
+  // Position of body command k (the (k+1)-th command strictly between s and
+  // e of body mask b).
+  __host__ __device__ __forceinline__ static int body_pos(const Mask128 &b, int s, int k) {
+    int p = s;
+    for (int k2 = 0; k2 <= k; k2++) p = mask_next(b, p + 1);
+    return p;
+  }
+
+  // A loop whose body is one run of '+' or '-' on the byte under h0 (outside
+  // the loop's code) counts that byte: each iteration adds d, and the ']'
+  // leaves once the byte is zero (under the null mask).  The iterations until
+  // then (all the step limit allows when it never is) are taken at once, the
+  // byte written once.  Returns 1 when the program ended, 0 otherwise.
+  __host__ __device__ __forceinline__ int count_loop(const LaneBytes t, const LaneBytes snapa,
+                                                     const LaneNp np,
+                                                     const uint8_t *__restrict__ optab, int s,
+                                                     int e, int m, uint32_t len) {
+    const int r = static_cast<int>((rcls >> 4) & 15) + 1;
+    const uint32_t d = static_cast<uint32_t>((rcls & 15) == kPlus ? r : -r);
+    const uint32_t lim = (kStepLimit - i) / len;  // whole iterations left, >= 1
+    const uint32_t kmax = lim < 256 ? lim : 256;  // the byte's values repeat after 256
+    uint32_t k = 1;
+    bool found = false;
+    for (; k <= kmax; k++) {
+      if (((v0 + k * d) & kNullMask) == 0) {
+        found = true;
+        break;
+      }
+    }
+    if (!found) k = lim;
+    const uint32_t v = (v0 + k * d) & 0xFF;
+    used0 = true;
+    write_fast(t, snapa, np, optab, h0, v0, v);
+    v0 = v;
+    if (h0 == h1) v1 = v;
+    i += k * len;
+    nskip += k * (len - 1 - static_cast<uint32_t>(m));
+    if (found) {  // the k-th ']' falls through
+      rpk = 0;
+      pc = e + 1;
+      if (pc >= kPair || i >= kStepLimit) return 1;
+      nxt = np.get(pc);
+      return 0;
+    }
+    pc = s + 1;
+    return i >= kStepLimit ? 1 : 0;
   }
 
   // A loop whose body only moves heads changes no byte, so its iterations
@@ -484,6 +539,7 @@ struct BffMachine {
       const int r = scan_loop(t, np, s, e, m, len);
       if (r >= 0) return r == 1;
     }
+    if ((rpk & kCountLoop) && (h0 < s || h0 > e)) return count_loop(t, snapa, np, optab, s, e, m, len) == 1;
     // The body's ops.
     int j = 0;
     for (uint64_t ops = rcls; ops != 0; ops >>= 8, j++) {
@@ -499,12 +555,25 @@ struct BffMachine {
         }
         continue;
       }
+      if (r > 1 && c <= kMinus && h0 >= s && h0 <= e) {
+        // A run of '+' / '-' on a byte of the loop's own code: leave the
+        // replay before its first command (body command k) and step it.
+        int k = 0;
+        for (int o2 = 0; o2 < j; o2++) k += static_cast<int>((rcls >> (8 * o2 + 4)) & 15) + 1;
+        const int p = body_pos(between(cmd, s, e), s, k);
+        i += static_cast<uint32_t>(p - 1 - s);
+        nskip += static_cast<uint32_t>(p - 1 - s - k);
+        rpk = 0;
+        pc = p;
+        nxt = entry_at(t, optab, p);
+        return false;
+      }
       used0 = true;
       const bool to1 = c == kCopy01;
       if (c >= kCopy01) used1 = true;
       const int a = to1 ? h1 : h0;
       const uint32_t o = to1 ? v1 : v0;
-      const uint32_t v = (c == kPlus ? v0 + 1 : c == kMinus ? v0 - 1 : to1 ? v0 : v1) & 0xFF;
+      const uint32_t v = (c == kPlus ? v0 + r : c == kMinus ? v0 - r : to1 ? v0 : v1) & 0xFF;
       if (to1) v1 = v; else v0 = v;
       if (h0 == h1) v0 = v1 = v;
       const int w = write_fast(t, snapa, np, optab, a, o, v);
@@ -521,8 +590,7 @@ struct BffMachine {
         for (int o2 = 0; o2 < j; o2++) k += static_cast<int>((rcls >> (8 * o2 + 4)) & 15) + 1;
         Mask128 body = between(cmd, s, e);
         if (a > s && a < e) mask_assign(body, a, w == 2);
-        int p = s;
-        for (int k2 = 0; k2 <= k; k2++) p = mask_next(body, p + 1);
+        const int p = body_pos(body, s, k);
         i += static_cast<uint32_t>(p - s);
         nskip += static_cast<uint32_t>(p - s - (k + 1));
         rpk = 0;

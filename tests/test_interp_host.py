@@ -99,6 +99,9 @@ CRAFTED = {
                     # runs that replay merges (head moves, repeated copies)
                     b"+[}" + b"," * 12 + b"q.q]", b"+[>>>>+]", b"+[<<<<<<<<<-]", b"+[}}}.,,,,]",
                     b"+[" + b">" * 20 + b"+" + b"<" * 19 + b"]", b"+[{{{{" + b"." * 17 + b"]",
+                    # counters: runs of '+' / '-' on one byte, also on the loop's own code
+                    b"+[---]", b"-[+++++]", b"+[" + b"-q" * 7 + b"]", b"[---]", b"[--]q",
+                    b"+[<" + b"+" * 9 + b">]", b"+[-" + b"q" * 30 + b"--]" + b"+" * 8,
                     # a tape that ran 6241 loop iterations of an h1-drift loop
                     bytes.fromhex(
                         "515b7d7b7b7d7d7b807d7d197b7d7d7b7b7d7d7b7b7d7d7b7b7dba7b7b7d7d7b7b7d7d"
