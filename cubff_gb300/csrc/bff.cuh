@@ -395,6 +395,27 @@ struct BffMachine {
     const Mask128 brk = between(Mask128{opn.lo | cls.lo, opn.hi | cls.hi}, s, e);
     if (brk.lo | brk.hi) return;
     const int m = popc64(body.lo) + popc64(body.hi);
+    // A body of head moves only: its net moves are all that matters.
+    {
+      int q = s, d0 = 0, d1 = 0;
+      bool moves = true;
+      for (int k = 0; k < m && moves; k++) {
+        const uint32_t en = np.get(q + 1);
+        q = static_cast<int>(en >> 4);
+        const uint32_t c = en & 15;
+        moves = c >= kDec0;
+        if (c == kInc0) d0++;
+        else if (c == kDec0) d0--;
+        else if (c == kInc1) d1++;
+        else if (c == kDec1) d1--;
+      }
+      if (moves) {
+        rcls = static_cast<uint64_t>(d0 & (kPair - 1)) | static_cast<uint64_t>(d1 & (kPair - 1)) << 8;
+        rpk = static_cast<uint32_t>(s) | (static_cast<uint32_t>(e) << 8) |
+              (static_cast<uint32_t>(m) << 16) | kScanLoop;
+        return;
+      }
+    }
     uint64_t ops = 0;
     int n = 0;             // ops so far
     uint32_t last = 16;    // op of the current run (16 = none)
@@ -415,13 +436,10 @@ struct BffMachine {
         cnt = 1;
       }
     }
-    bool moves_only = true;
-    for (int o2 = 0; o2 < n; o2++) moves_only &= ((ops >> (8 * o2)) & 15) >= kDec0;
     const bool counter = n == 1 && ((ops & 15) == kPlus || (ops & 15) == kMinus);
     rcls = ops;
     rpk = static_cast<uint32_t>(s) | (static_cast<uint32_t>(e) << 8) |
-          (static_cast<uint32_t>(m) << 16) | (moves_only ? kScanLoop : 0u) |
-          (counter ? kCountLoop : 0u);
+          (static_cast<uint32_t>(m) << 16) | (counter ? kCountLoop : 0u);
   }
 
   // Position of body command k (the (k+1)-th command strictly between s and
@@ -481,15 +499,8 @@ struct BffMachine {
   // the test never changes).
   __host__ __device__ __forceinline__ int scan_loop(const LaneBytes t, const LaneNp np, int s,
                                                     int e, int m, uint32_t len) {
-    int d0 = 0, d1 = 0;
-    for (uint64_t w = rcls; w; w >>= 8) {
-      const uint32_t c = w & 15;
-      const int r = static_cast<int>((w >> 4) & 15) + 1;
-      if (c == kInc0) d0 += r;
-      else if (c == kDec0) d0 -= r;
-      else if (c == kInc1) d1 += r;
-      else d1 -= r;
-    }
+    const int d0 = static_cast<int>(rcls & (kPair - 1));         // net moves, mod 128
+    const int d1 = static_cast<int>((rcls >> 8) & (kPair - 1));
     if ((d0 & (kPair - 1)) == 0) return -1;
     const uint32_t lim = (kStepLimit - i) / len;  // whole iterations left, >= 1
     const uint32_t kmax = lim < kPair ? lim : kPair;
@@ -538,11 +549,17 @@ struct BffMachine {
     if (rpk & kScanLoop) {
       const int r = scan_loop(t, np, s, e, m, len);
       if (r >= 0) return r == 1;
+      // h0 returns to itself each iteration: one iteration, by its net moves.
+      const int d1 = static_cast<int>((rcls >> 8) & (kPair - 1));
+      if (d1) {
+        h1 = (h1 + d1) & (kPair - 1);
+        v1 = t.get(h1);
+      }
     }
     if ((rpk & kCountLoop) && (h0 < s || h0 > e)) return count_loop(t, snapa, np, optab, s, e, m, len) == 1;
     // The body's ops.
     int j = 0;
-    for (uint64_t ops = rcls; ops != 0; ops >>= 8, j++) {
+    for (uint64_t ops = (rpk & kScanLoop) ? 0 : rcls; ops != 0; ops >>= 8, j++) {
       const uint32_t c = ops & 15;
       const int r = static_cast<int>((ops >> 4) & 15) + 1;  // commands merged into this op
       if (c >= kDec0) {

@@ -102,6 +102,9 @@ CRAFTED = {
                     # counters: runs of '+' / '-' on one byte, also on the loop's own code
                     b"+[---]", b"-[+++++]", b"+[" + b"-q" * 7 + b"]", b"[---]", b"[--]q",
                     b"+[<" + b"+" * 9 + b">]", b"+[-" + b"q" * 30 + b"--]" + b"+" * 8,
+                    # scans whose moves cancel in part (net moves only matter)
+                    b"+[<><><><>>" + b"q" * 3 + b"<><>{}{]", b"+[<>]", b"+[{<}>}]",
+                    b"+[>><<<><><>>>>" + b"q" * 9 + b"<]",
                     # a tape that ran 6241 loop iterations of an h1-drift loop
                     bytes.fromhex(
                         "515b7d7b7b7d7d7b807d7d197b7d7d7b7b7d7d7b7b7d7d7b7b7dba7b7b7d7d7b7b7d7d"
