@@ -416,38 +416,62 @@ struct BffMachine {
         return;
       }
     }
+    // Otherwise up to 8 ops: a run of head moves becomes its net moves (one
+    // op per head, |net| <= 16), a run of one copy or of one of '+' / '-'
+    // one op.  The position of each op's first command is kept in the spare
+    // entries of np (np[kPair + 1 + op]) for leaving the replay mid-body.
     uint64_t ops = 0;
-    int n = 0;             // ops so far
-    uint32_t last = 16;    // op of the current run (16 = none)
+    int n = 0;              // ops so far
+    uint32_t last = 16;     // value op of the current run (16 = none)
     uint32_t cnt = 0;
+    int md0 = 0, md1 = 0;   // net moves of the current run of moves
+    int mpos = -1;          // its first command (-1 = no run)
+    bool ok = true;
+    // Appends op c with count r (1..16) whose first command is at p.
+    auto emit = [&](uint32_t c, int r, int p) {
+      if (n == 8 || r > 16) {
+        ok = false;
+        return;
+      }
+      ops |= (static_cast<uint64_t>(c) | static_cast<uint64_t>(r - 1) << 4) << (8 * n);
+      np.set(kPair + 1 + n, static_cast<uint32_t>(p));
+      n++;
+    };
+    auto flush_moves = [&]() {
+      if (mpos < 0) return;
+      if (md0) emit(md0 > 0 ? kInc0 : kDec0, md0 > 0 ? md0 : -md0, mpos);
+      if (md1) emit(md1 > 0 ? kInc1 : kDec1, md1 > 0 ? md1 : -md1, mpos);
+      md0 = md1 = 0;
+      mpos = -1;
+    };
     int q = s;
-    for (int k = 0; k < m; k++) {
+    for (int k = 0; k < m && ok; k++) {
       const uint32_t en = np.get(q + 1);
       q = static_cast<int>(en >> 4);
       const uint32_t c = en & 15;
+      if (c >= kDec0) {
+        if (mpos < 0) mpos = q;
+        md0 += c == kInc0 ? 1 : c == kDec0 ? -1 : 0;
+        md1 += c == kInc1 ? 1 : c == kDec1 ? -1 : 0;
+        last = 16;
+        continue;
+      }
+      flush_moves();
       if (c == last && mergeable(c) && cnt < 16) {
         cnt++;
         ops += 1ull << (8 * (n - 1) + 4);
       } else {
-        if (n == 8) return;
-        ops |= static_cast<uint64_t>(c) << (8 * n);
-        n++;
+        emit(c, 1, q);
         last = c;
         cnt = 1;
       }
     }
+    flush_moves();
+    if (!ok) return;
     const bool counter = n == 1 && ((ops & 15) == kPlus || (ops & 15) == kMinus);
     rcls = ops;
     rpk = static_cast<uint32_t>(s) | (static_cast<uint32_t>(e) << 8) |
           (static_cast<uint32_t>(m) << 16) | (counter ? kCountLoop : 0u);
-  }
-
-  // Position of body command k (the (k+1)-th command strictly between s and
-  // e of body mask b).
-  __host__ __device__ __forceinline__ static int body_pos(const Mask128 &b, int s, int k) {
-    int p = s;
-    for (int k2 = 0; k2 <= k; k2++) p = mask_next(b, p + 1);
-    return p;
   }
 
   // A loop whose body is one run of '+' or '-' on the byte under h0 (outside
@@ -575,9 +599,9 @@ struct BffMachine {
       if (r > 1 && c <= kMinus && h0 >= s && h0 <= e) {
         // A run of '+' / '-' on a byte of the loop's own code: leave the
         // replay before its first command (body command k) and step it.
-        int k = 0;
-        for (int o2 = 0; o2 < j; o2++) k += static_cast<int>((rcls >> (8 * o2 + 4)) & 15) + 1;
-        const int p = body_pos(between(cmd, s, e), s, k);
+        const int p = static_cast<int>(np.get(kPair + 1 + j));
+        const Mask128 before = between(cmd, s, p);  // the body's commands before p
+        const int k = popc64(before.lo) + popc64(before.hi);
         i += static_cast<uint32_t>(p - 1 - s);
         nskip += static_cast<uint32_t>(p - 1 - s - k);
         rpk = 0;
@@ -600,14 +624,13 @@ struct BffMachine {
       }
       if (w && a >= s && a <= e) {
         // The loop changed its own code: stop replaying after this command
-        // (the first of its op; a repeat writes nothing).  It is body
-        // command k = the commands of the ops before it, at the (k+1)-th
-        // position of the body as it was (a's bit as before the write).
-        int k = 0;
-        for (int o2 = 0; o2 < j; o2++) k += static_cast<int>((rcls >> (8 * o2 + 4)) & 15) + 1;
-        Mask128 body = between(cmd, s, e);
-        if (a > s && a < e) mask_assign(body, a, w == 2);
-        const int p = body_pos(body, s, k);
+        // (the first of its op, at p; a repeat writes nothing).  The body's
+        // commands before p are counted as they were (a's bit as before the
+        // write).
+        const int p = static_cast<int>(np.get(kPair + 1 + j));
+        Mask128 before = between(cmd, s, p);
+        if (a > s && a < p) mask_assign(before, a, w == 2);
+        const int k = popc64(before.lo) + popc64(before.hi);  // commands before p
         i += static_cast<uint32_t>(p - s);
         nskip += static_cast<uint32_t>(p - s - (k + 1));
         rpk = 0;

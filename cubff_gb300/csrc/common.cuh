@@ -69,11 +69,14 @@ struct LaneBytes {
   }
 };
 
-// One thread's array of kPair + 1 16-bit entries (the BFF next-command
-// array, bff.cuh).  Entry p of thread tid sits at element p * 128 + tid of a
-// block of 128 threads: a warp's 32 lanes read 64 consecutive bytes for any
-// common p.  Per block of 128 threads: kNpBytes.
-constexpr int kNpBytes = (kPair + 1) * 128 * 2;
+// One thread's array of kNpEntries 16-bit entries (the BFF next-command
+// array, bff.cuh: kPair + 1 entries, then kNpSpare entries of loop-replay
+// state).  Entry p of thread tid sits at element p * 128 + tid of a block of
+// 128 threads: a warp's 32 lanes read 64 consecutive bytes for any common p.
+// Per block of 128 threads: kNpBytes.
+constexpr int kNpSpare = 8;
+constexpr int kNpEntries = kPair + 1 + kNpSpare;
+constexpr int kNpBytes = kNpEntries * 128 * 2;
 
 struct LaneNp {
   uint16_t *s;    // nullptr: no array (the interpreter stays in its basic mode)
