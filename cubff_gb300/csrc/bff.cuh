@@ -416,9 +416,9 @@ struct BffMachine {
         return;
       }
     }
-    // Otherwise up to 8 ops: a run of head moves becomes its net moves (one
-    // op per head, |net| <= 16), a run of one copy or of one of '+' / '-'
-    // one op.  The position of each op's first command is kept in the spare
+    // Otherwise up to 8 ops: a run of head moves becomes its net moves (ops
+    // of at most 16 per head), a run of one copy or of one of '+' / '-' one
+    // op.  The position of each op's first command is kept in the spare
     // entries of np (np[kPair + 1 + op]) for leaving the replay mid-body.
     uint64_t ops = 0;
     int n = 0;              // ops so far
@@ -437,10 +437,20 @@ struct BffMachine {
       np.set(kPair + 1 + n, static_cast<uint32_t>(p));
       n++;
     };
+    // A net move (mod 128, as the smallest |d| <= 64) in ops of at most 16.
+    auto emit_move = [&](int d, uint32_t inc, uint32_t dec) {
+      d &= kPair - 1;
+      if (d > kPair / 2) d -= kPair;
+      while (d != 0 && ok) {
+        const int r = d > 16 ? 16 : d < -16 ? -16 : d;
+        emit(r > 0 ? inc : dec, r > 0 ? r : -r, mpos);
+        d -= r;
+      }
+    };
     auto flush_moves = [&]() {
       if (mpos < 0) return;
-      if (md0) emit(md0 > 0 ? kInc0 : kDec0, md0 > 0 ? md0 : -md0, mpos);
-      if (md1) emit(md1 > 0 ? kInc1 : kDec1, md1 > 0 ? md1 : -md1, mpos);
+      emit_move(md0, kInc0, kDec0);
+      emit_move(md1, kInc1, kDec1);
       md0 = md1 = 0;
       mpos = -1;
     };
