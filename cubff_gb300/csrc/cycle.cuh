@@ -83,36 +83,5 @@ __host__ __device__ __forceinline__ int mask_prev(const Mask128 &m, int p) {
   return x ? 63 - clz64(x) : -1;
 }
 
-// Brent-schedule snapshot of an interpreter state (a, b, c identify the
-// control state; mods counts value-changing writes to tape and stack).
-struct CycleSnap {
-  int a = -1, b = 0, c = 0;
-  uint32_t mods = 0, i = 0, skip = 0;
-  uint32_t power = 1, lam = 0;
-
-  // Called at a step boundary right after a backward control transfer.
-  // Returns the number of raw steps to add (whole periods), updating *skip.
-  __host__ __device__ __forceinline__ uint32_t visit(int a_, int b_, int c_, uint32_t mods_, uint32_t i_,
-                                            uint32_t *skip_, uint32_t limit) {
-    uint32_t jump = 0;
-    if (a_ == a && b_ == b && c_ == c && mods_ == mods) {
-      const uint32_t period = i_ - i;
-      const uint32_t k = (limit - i_) / period;
-      jump = k * period;
-      *skip_ += k * (*skip_ - skip);
-    }
-    if (++lam == power) {
-      a = a_;
-      b = b_;
-      c = c_;
-      mods = mods_;
-      i = i_ + jump;
-      skip = *skip_;
-      power <<= 1;
-      lam = 0;
-    }
-    return jump;
-  }
-};
 
 }  // namespace cubff

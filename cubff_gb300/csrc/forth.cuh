@@ -7,10 +7,13 @@
 // stack (128 bytes) lives in shared memory in the same bank-per-lane layout as
 // the tape.
 //
-// Exact cycle fast-forward (cycle.cuh) at backward jumps: the state is
-// (pos, stack pointer, tape, stack contents); a push that stores the value
-// already in its slot and a write that stores the value already in its byte
-// change nothing, so only value-changing stores count as modifications.
+// Exact cycle fast-forward at backward jumps (Brent's schedule, as in
+// cycle.cuh): the state is (pos, stack pointer, stack contents, tape).  The
+// stack below the stack pointer is compared byte for byte with the
+// snapshot's (kept packed in a register, so only for stacks of at most 8);
+// the tape through a count of value-changing writes (a write that stores the
+// byte already there changes nothing).  Stack slots at or above the stack
+// pointer are not part of the state: a push overwrites them before any read.
 #pragma once
 
 #include "cycle.cuh"
@@ -31,30 +34,61 @@ template <bool kWithReset>
 struct ForthMachine {
   int pos, sp;
   bool overflow;
-  uint32_t i, nops, mods;
-  CycleSnap snap;
+  uint32_t i, nops, mods;  // mods: value-changing tape writes
+  // Brent-schedule snapshot taken at a backward jump.
+  int s_pos, s_sp;
+  uint32_t s_mods, s_i, s_nops, s_power, s_lam;
+  uint64_t s_stk;          // stack[0 .. s_sp) packed, byte j at bits 8j (s_sp <= 8)
 
   // Stack slots at or above sp hold bytes left by an earlier pair; they are
-  // never read before a push overwrites them, and a push compares against
-  // whatever the slot holds, so equal modification counts still imply equal
-  // stacks.
+  // never read before a push overwrites them.
   __host__ __device__ __forceinline__ void begin() {
     pos = sp = 0;
     overflow = false;
     i = nops = mods = 0;
-    snap = CycleSnap();
+    s_pos = -1;
+    s_sp = 0;
+    s_mods = s_i = s_nops = 0;
+    s_power = 1;
+    s_lam = 0;
+    s_stk = 0;
   }
 
   __host__ __device__ __forceinline__ void push(const LaneBytes stk, uint32_t v) {
-    v &= 0xFF;
     if (sp != kPair) {
-      if (stk.get(sp) != v) {
-        stk.set(sp, v);
-        mods++;
-      }
+      stk.set(sp, v & 0xFF);
       sp++;
     } else {
       overflow = true;
+    }
+  }
+
+  __host__ __device__ __forceinline__ uint64_t pack_stack(const LaneBytes stk) const {
+    uint64_t w = 0;
+    for (int j = 0; j < sp; j++) w |= static_cast<uint64_t>(stk.get(j)) << (8 * j);
+    return w;
+  }
+
+  // At a step boundary right after a backward jump: when the state equals
+  // the snapshot's, execution since the snapshot is periodic and whole periods
+  // are skipped (i += k * P, nops += k * the period's no-ops); the snapshot is
+  // renewed after 1, 2, 4, ... visits.
+  __host__ __device__ __forceinline__ void visit(const LaneBytes stk) {
+    if (pos == s_pos && sp == s_sp && mods == s_mods && pack_stack(stk) == s_stk) {
+      const uint32_t period = i - s_i;
+      const uint32_t k = (kStepLimit - i) / period;
+      i += k * period;
+      nops += k * (nops - s_nops);
+    }
+    if (++s_lam == s_power) {
+      s_pos = sp <= 8 ? pos : -1;  // larger stacks: no snapshot
+      s_sp = sp;
+      s_mods = mods;
+      s_i = i;
+      s_nops = nops;
+      s_stk = sp <= 8 ? pack_stack(stk) : 0;
+      s_power <<= 1;
+      s_lam = 0;
     }
   }
   __host__ __device__ __forceinline__ uint32_t pop(const LaneBytes stk) {
@@ -150,7 +184,7 @@ struct ForthMachine {
     i++;
     if (pos >= kPair || pos < 0 || overflow || i >= kStepLimit) return true;
     if (back) {
-      i += snap.visit(pos, sp, 0, mods, i, &nops, kStepLimit);
+      visit(stk);
       if (i >= kStepLimit) return true;
     }
     return false;
