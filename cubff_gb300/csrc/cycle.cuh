@@ -5,9 +5,11 @@
 // state (program counter, heads or stack, tape).  At each backward control
 // transfer the interpreter compares its state with a snapshot taken at an
 // earlier backward transfer (Brent's cycle-finding schedule: the snapshot is
-// renewed after 1, 2, 4, ... transfers).  Tape and stack equality is tracked
-// with a counter of value-changing writes: equal counters mean nothing changed
-// in between.  When the state repeats, execution from the snapshot onwards is
+// renewed after 1, 2, 4, ... transfers).  How equality of the tape (and the
+// stack) is established is up to each interpreter: BFF and SUBLEQ compare the
+// positions written since the snapshot with their saved values, Forth compares
+// the stack byte for byte and counts value-changing tape writes.  When the
+// state repeats, execution from the snapshot onwards is
 // periodic with period P = steps since the snapshot, so whole periods are
 // skipped: the step counter advances by k*P and the no-op counter by k times
 // the no-ops of one period, k = floor(remaining steps / P).  A repeating state
