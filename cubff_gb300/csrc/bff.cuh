@@ -377,6 +377,7 @@ struct BffMachine {
 
   static constexpr uint32_t kScanLoop = 1u << 23;
   static constexpr uint32_t kCountLoop = 1u << 24;
+  static constexpr uint32_t kFixedTest = 1u << 25;
 
   // Ops that a run of may merge into one replay op: head moves, copies (a
   // repeat copies a value onto itself) and '+' / '-' (a run adds its length
@@ -479,9 +480,74 @@ struct BffMachine {
     flush_moves();
     if (!ok) return;
     const bool counter = n == 1 && ((ops & 15) == kPlus || (ops & 15) == kMinus);
+    // A body of head moves and '+' / '-' whose h0 moves cancel, none of whose
+    // '+' / '-' hits the byte under h0 at the ']': the ']' tests the same
+    // unchanged byte every iteration.
+    bool fixed = !counter;
+    int off = 0;
+    for (int o2 = 0; o2 < n && fixed; o2++) {
+      const uint32_t c = (ops >> (8 * o2)) & 15;
+      const int r = static_cast<int>((ops >> (8 * o2 + 4)) & 15) + 1;
+      if (c == kInc0) off += r;
+      else if (c == kDec0) off -= r;
+      else if (c == kPlus || c == kMinus) fixed = (off & (kPair - 1)) != 0;
+      else if (c != kInc1 && c != kDec1) fixed = false;
+    }
+    fixed = fixed && (off & (kPair - 1)) == 0;
     rcls = ops;
     rpk = static_cast<uint32_t>(s) | (static_cast<uint32_t>(e) << 8) |
-          (static_cast<uint32_t>(m) << 16) | (counter ? kCountLoop : 0u);
+          (static_cast<uint32_t>(m) << 16) | (counter ? kCountLoop : 0u) |
+          (fixed ? kFixedTest : 0u);
+  }
+
+  // A loop of kFixedTest whose ']' was taken once takes it every time: it
+  // runs until the step limit.  Its bytes change by the same amounts every
+  // iteration (each '+' / '-' hits a byte at a fixed offset from h0), so all
+  // the whole iterations the limit allows are taken at once: each of those
+  // bytes gains k times its change per iteration, h1 drifts by k times its
+  // net move.  Returns 1 when the program ended, 0 when the loop was taken
+  // over, -1 when a byte it changes lies in the loop's code (those steps must
+  // stay exact, one by one).
+  __host__ __device__ __forceinline__ int fixed_loop(const LaneBytes t, const LaneBytes snapa,
+                                                     const LaneNp np,
+                                                     const uint8_t *__restrict__ optab, int s,
+                                                     int e, int m, uint32_t len) {
+    int off = 0;
+    for (uint64_t w = rcls; w; w >>= 8) {
+      const uint32_t c = w & 15;
+      const int r = static_cast<int>((w >> 4) & 15) + 1;
+      if (c == kInc0) off += r;
+      else if (c == kDec0) off -= r;
+      else if (c == kPlus || c == kMinus) {
+        const int a = (h0 + off) & (kPair - 1);
+        if (a >= s && a <= e) return -1;
+      }
+    }
+    const uint32_t k = (kStepLimit - i) / len;  // whole iterations left, >= 1
+    int d1 = 0;
+    off = 0;
+    for (uint64_t w = rcls; w; w >>= 8) {
+      const uint32_t c = w & 15;
+      const int r = static_cast<int>((w >> 4) & 15) + 1;
+      if (c == kInc0) off += r;
+      else if (c == kDec0) off -= r;
+      else if (c == kInc1) d1 += r;
+      else if (c == kDec1) d1 -= r;
+      else {
+        const int a = (h0 + off) & (kPair - 1);
+        const uint32_t o = t.get(a);
+        const uint32_t v = (o + k * static_cast<uint32_t>(c == kPlus ? r : -r)) & 0xFF;
+        write_fast(t, snapa, np, optab, a, o, v);
+      }
+    }
+    used0 = true;
+    h1 = (h1 + static_cast<int>(k) * d1) & (kPair - 1);
+    v0 = t.get(h0);
+    v1 = t.get(h1);
+    i += k * len;
+    nskip += k * (len - 1 - static_cast<uint32_t>(m));
+    pc = s + 1;
+    return i >= kStepLimit ? 1 : 0;
   }
 
   // A loop whose body is one run of '+' or '-' on the byte under h0 (outside
@@ -591,6 +657,10 @@ struct BffMachine {
       }
     }
     if ((rpk & kCountLoop) && (h0 < s || h0 > e)) return count_loop(t, snapa, np, optab, s, e, m, len) == 1;
+    if (rpk & kFixedTest) {
+      const int r = fixed_loop(t, snapa, np, optab, s, e, m, len);
+      if (r >= 0) return r == 1;
+    }
     // The body's ops.
     int j = 0;
     for (uint64_t ops = (rpk & kScanLoop) ? 0 : rcls; ops != 0; ops >>= 8, j++) {

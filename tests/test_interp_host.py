@@ -105,6 +105,9 @@ CRAFTED = {
                     # scans whose moves cancel in part (net moves only matter)
                     b"+[<><><><>>" + b"q" * 3 + b"<><>{}{]", b"+[<>]", b"+[{<}>}]",
                     b"+[>><<<><><>>>>" + b"q" * 9 + b"<]",
+                    # fixed tests: the ']' reads a byte the body never changes
+                    b"+[<+>]", b"+[<<+>-<<+>>>]" + b"q" * 4, b"+[>+<]", b"+[>>++<<}]",
+                    b"+[<" + b"q" * 20 + b"---}>]", b"-[<+<+>>]" + b"+" * 30,
                     # a tape that ran 6241 loop iterations of an h1-drift loop
                     bytes.fromhex(
                         "515b7d7b7b7d7d7b807d7d197b7d7d7b7b7d7d7b7b7d7d7b7b7dba7b7b7d7d7b7b7d7d"
