@@ -378,6 +378,7 @@ struct BffMachine {
   static constexpr uint32_t kScanLoop = 1u << 23;
   static constexpr uint32_t kCountLoop = 1u << 24;
   static constexpr uint32_t kFixedTest = 1u << 25;
+  static constexpr int kReplayBatch = 8;  // replayed iterations per step call
 
   // Ops that a run of may merge into one replay op: head moves, copies (a
   // repeat copies a value onto itself) and '+' / '-' (a run adds its length
@@ -649,94 +650,110 @@ struct BffMachine {
     if (rpk & kScanLoop) {
       const int r = scan_loop(t, np, s, e, m, len);
       if (r >= 0) return r == 1;
-      // h0 returns to itself each iteration: one iteration, by its net moves.
-      const int d1 = static_cast<int>((rcls >> 8) & (kPair - 1));
-      if (d1) {
-        h1 = (h1 + d1) & (kPair - 1);
-        v1 = t.get(h1);
-      }
     }
     if ((rpk & kCountLoop) && (h0 < s || h0 > e)) return count_loop(t, snapa, np, optab, s, e, m, len) == 1;
     if (rpk & kFixedTest) {
       const int r = fixed_loop(t, snapa, np, optab, s, e, m, len);
       if (r >= 0) return r == 1;
     }
-    // The body's ops.
-    int j = 0;
-    for (uint64_t ops = (rpk & kScanLoop) ? 0 : rcls; ops != 0; ops >>= 8, j++) {
-      const uint32_t c = ops & 15;
-      const int r = static_cast<int>((ops >> 4) & 15) + 1;  // commands merged into this op
-      if (c >= kDec0) {
-        if (c <= kInc0) {
-          h0 = (h0 + (c == kInc0 ? r : -r)) & (kPair - 1);
-          v0 = t.get(h0);
-        } else {
-          h1 = (h1 + (c == kInc1 ? r : -r)) & (kPair - 1);
-          v1 = t.get(h1);
-        }
-        continue;
-      }
-      if (r > 1 && c <= kMinus && h0 >= s && h0 <= e) {
-        // A run of '+' / '-' on a byte of the loop's own code: leave the
-        // replay before its first command (body command k) and step it.
-        const int p = static_cast<int>(np.get(kPair + 1 + j));
-        const Mask128 before = between(cmd, s, p);  // the body's commands before p
-        const int k = popc64(before.lo) + popc64(before.hi);
-        i += static_cast<uint32_t>(p - 1 - s);
-        nskip += static_cast<uint32_t>(p - 1 - s - k);
+    // Up to kReplayBatch iterations.
+    for (int it = 0; it < kReplayBatch; it++) {
+      if (it > 0 && i + len > kStepLimit) {
         rpk = 0;
-        pc = p;
-        nxt = entry_at(t, optab, p);
-        return false;
-      }
-      used0 = true;
-      const bool to1 = c == kCopy01;
-      if (c >= kCopy01) used1 = true;
-      const int a = to1 ? h1 : h0;
-      const uint32_t o = to1 ? v1 : v0;
-      const uint32_t v = (c == kPlus ? v0 + r : c == kMinus ? v0 - r : to1 ? v0 : v1) & 0xFF;
-      if (to1) v1 = v; else v0 = v;
-      if (h0 == h1) v0 = v1 = v;
-      const int w = write_fast(t, snapa, np, optab, a, o, v);
-      if (kLogic == kLogicSelfmove && c == kCopy10) {
-        h1 = (h1 + 1) & (kPair - 1);
-        v1 = t.get(h1);
-      }
-      if (w && a >= s && a <= e) {
-        // The loop changed its own code: stop replaying after this command
-        // (the first of its op, at p; a repeat writes nothing).  The body's
-        // commands before p are counted as they were (a's bit as before the
-        // write).
-        const int p = static_cast<int>(np.get(kPair + 1 + j));
-        Mask128 before = between(cmd, s, p);
-        if (a > s && a < p) mask_assign(before, a, w == 2);
-        const int k = popc64(before.lo) + popc64(before.hi);  // commands before p
-        i += static_cast<uint32_t>(p - s);
-        nskip += static_cast<uint32_t>(p - s - (k + 1));
-        rpk = 0;
-        pc = p + 1;
+        pc = s + 1;
         nxt = np.get(pc);
         return false;
       }
+      if (rpk & kScanLoop) {
+        // h0 returns to itself each iteration: the iteration is its net moves.
+        const int d1 = static_cast<int>((rcls >> 8) & (kPair - 1));
+        if (d1) {
+          h1 = (h1 + d1) & (kPair - 1);
+          v1 = t.get(h1);
+        }
+      }
+      // The body's ops.
+      int j = 0;
+      for (uint64_t ops = (rpk & kScanLoop) ? 0 : rcls; ops != 0; ops >>= 8, j++) {
+        const uint32_t c = ops & 15;
+        const int r = static_cast<int>((ops >> 4) & 15) + 1;  // commands merged into this op
+        if (c >= kDec0) {
+          if (c <= kInc0) {
+            h0 = (h0 + (c == kInc0 ? r : -r)) & (kPair - 1);
+            v0 = t.get(h0);
+          } else {
+            h1 = (h1 + (c == kInc1 ? r : -r)) & (kPair - 1);
+            v1 = t.get(h1);
+          }
+          continue;
+        }
+        if (r > 1 && c <= kMinus && h0 >= s && h0 <= e) {
+          // A run of '+' / '-' on a byte of the loop's own code: leave the
+          // replay before its first command (body command k) and step it.
+          const int p = static_cast<int>(np.get(kPair + 1 + j));
+          const Mask128 before = between(cmd, s, p);  // the body's commands before p
+          const int k = popc64(before.lo) + popc64(before.hi);
+          i += static_cast<uint32_t>(p - 1 - s);
+          nskip += static_cast<uint32_t>(p - 1 - s - k);
+          rpk = 0;
+          pc = p;
+          nxt = entry_at(t, optab, p);
+          return false;
+        }
+        used0 = true;
+        const bool to1 = c == kCopy01;
+        if (c >= kCopy01) used1 = true;
+        const int a = to1 ? h1 : h0;
+        const uint32_t o = to1 ? v1 : v0;
+        const uint32_t v = (c == kPlus ? v0 + r : c == kMinus ? v0 - r : to1 ? v0 : v1) & 0xFF;
+        if (to1) v1 = v; else v0 = v;
+        if (h0 == h1) v0 = v1 = v;
+        const int w = write_fast(t, snapa, np, optab, a, o, v);
+        if (kLogic == kLogicSelfmove && c == kCopy10) {
+          h1 = (h1 + 1) & (kPair - 1);
+          v1 = t.get(h1);
+        }
+        if (w && a >= s && a <= e) {
+          // The loop changed its own code: stop replaying after this command
+          // (the first of its op, at p; a repeat writes nothing).  The body's
+          // commands before p are counted as they were (a's bit as before the
+          // write).
+          const int p = static_cast<int>(np.get(kPair + 1 + j));
+          Mask128 before = between(cmd, s, p);
+          if (a > s && a < p) mask_assign(before, a, w == 2);
+          const int k = popc64(before.lo) + popc64(before.hi);  // commands before p
+          i += static_cast<uint32_t>(p - s);
+          nskip += static_cast<uint32_t>(p - s - (k + 1));
+          rpk = 0;
+          pc = p + 1;
+          nxt = np.get(pc);
+          return false;
+        }
+      }
+      // The ']' at e: the iteration's raw steps and no-ops, then its test.
+      i += len;
+      nskip += len - 1 - m;
+      used0 = true;
+      if ((v0 & kNullMask) == 0) {
+        rpk = 0;
+        pc = e + 1;
+        if (pc >= kPair || i >= kStepLimit) return true;
+        nxt = np.get(pc);
+        return false;
+      }
+      pc = s + 1;
+      if (i >= kStepLimit) return true;
+      // The cycle check runs on every kReplayBatch-th iteration only: states
+      // sampled at a fixed stride repeat when the loop does, and a repeat found
+      // on the samples is a repeat of the loop.
+      if (it == kReplayBatch - 1) {
+        const int g0 = h0, g1 = h1;
+        visit(t, snapa);
+        if (i >= kStepLimit) return true;
+        if (h0 != g0) v0 = t.get(h0);
+        if (h1 != g1) v1 = t.get(h1);
+      }
     }
-    // The ']' at e: the iteration's raw steps and no-ops, then its test.
-    i += len;
-    nskip += len - 1 - m;
-    used0 = true;
-    if ((v0 & kNullMask) == 0) {
-      rpk = 0;
-      pc = e + 1;
-      if (pc >= kPair || i >= kStepLimit) return true;
-      nxt = np.get(pc);
-      return false;
-    }
-    pc = s + 1;
-    if (i >= kStepLimit) return true;
-    const int g0 = h0, g1 = h1;
-    visit(t, snapa);
-    if (i >= kStepLimit) return true;
-    if (h0 != g0) v0 = t.get(h0);
-    if (h1 != g1) v1 = t.get(h1);
     return false;
   }
 
