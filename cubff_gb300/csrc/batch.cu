@@ -57,7 +57,9 @@ int cubff_engine::reserve_pipe(size_t groups, size_t entries) {
     d_queue = nullptr;
     queue_cap = 0;
     CUBFF_CUDA_TRY(cudaMalloc(&d_queue, entries * sizeof(uint32_t)));
-    CUBFF_CUDA_TRY(cudaMemset(d_queue, 0, entries * sizeof(uint32_t)));
+    // On the engine's stream: the pipelined kernels run on non-blocking
+    // streams, which a memset on the legacy default stream does not order.
+    CUBFF_CUDA_TRY(cudaMemsetAsync(d_queue, 0, entries * sizeof(uint32_t), stream));
     queue_cap = entries;
   }
   return CUBFF_OK;

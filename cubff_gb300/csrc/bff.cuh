@@ -378,6 +378,10 @@ struct BffMachine {
   static constexpr uint32_t kScanLoop = 1u << 23;
   static constexpr uint32_t kCountLoop = 1u << 24;
   static constexpr uint32_t kFixedTest = 1u << 25;
+  // Copy sweeps (copy_sweep) are off for bff_selfmove, whose copies move h1
+  // (they are not a fixed-destination sweep), and whose pipelined kernel
+  // stays built from the code it was validated with.
+  static constexpr uint32_t kCopySweep = 1u << 26;
   static constexpr int kReplayBatch = 8;  // replayed iterations per step call
 
   // Ops that a run of may merge into one replay op: head moves, copies (a
@@ -495,10 +499,43 @@ struct BffMachine {
       else if (c != kInc1 && c != kDec1) fixed = false;
     }
     fixed = fixed && (off & (kPair - 1)) == 0;
+    // A body of head moves and at most two copies of one direction, all
+    // writing the same byte (the destination head is at the same offset at
+    // each copy and has no net move), whose source head sweeps.  A copy of
+    // the other direction right after a copy writes back the byte it just
+    // read: it changes nothing.
+    bool sweep = !counter && !fixed;
+    if constexpr (kLogic != kLogicSelfmove) {  // (bff_selfmove: see kCopySweep)
+      int o0 = 0, o1 = 0, wo = 0, nc = 0;
+      uint32_t dir = 16, prev = 16;
+      for (int o2 = 0; o2 < n && sweep; o2++) {
+        const uint32_t c = (ops >> (8 * o2)) & 15;
+        const int r = static_cast<int>((ops >> (8 * o2 + 4)) & 15) + 1;
+        if (c == kInc0) o0 += r;
+        else if (c == kDec0) o0 -= r;
+        else if (c == kInc1) o1 += r;
+        else if (c == kDec1) o1 -= r;
+        else if (c != kCopy01 && c != kCopy10) sweep = false;
+        else if (dir == 16 || c == dir) {
+          const int d = (c == kCopy01 ? o1 : o0) & (kPair - 1);
+          sweep = nc < 2 && (nc == 0 || d == wo);
+          dir = c;
+          wo = d;
+          nc++;
+        } else {
+          sweep = prev == dir;
+        }
+        prev = c;
+      }
+      sweep = sweep && nc > 0 && ((dir == kCopy01 ? o1 : o0) & (kPair - 1)) == 0 &&
+              ((dir == kCopy01 ? o0 : o1) & (kPair - 1)) != 0;
+    } else {
+      sweep = false;
+    }
     rcls = ops;
     rpk = static_cast<uint32_t>(s) | (static_cast<uint32_t>(e) << 8) |
           (static_cast<uint32_t>(m) << 16) | (counter ? kCountLoop : 0u) |
-          (fixed ? kFixedTest : 0u);
+          (fixed ? kFixedTest : 0u) | (sweep ? kCopySweep : 0u);
   }
 
   // A loop of kFixedTest whose ']' was taken once takes it every time: it
@@ -634,6 +671,87 @@ struct BffMachine {
     return i >= kStepLimit ? 1 : 0;
   }
 
+  // A loop of kCopySweep: every iteration writes one byte w with bytes that
+  // the sweeping source head reads.  As only w changes, the iterations are
+  // followed on positions alone: a copy reads the byte as it was, or w's
+  // value where it reads w (the value last copied), and the ']' tests the
+  // byte under h0 the same way.  From iteration 129 on, the positions and w's
+  // value repeat those of 128 iterations earlier (the heads move by the same
+  // amount mod 128 each iteration): 257 iterations without a zero test mean
+  // none ever comes, and whole periods of 128 are skipped.  w is then written
+  // once, with its final value.  Returns as scan_loop does; -1 (nothing done)
+  // when w lies in the loop's own code.
+  __host__ __device__ __forceinline__ int copy_sweep(const LaneBytes t, const LaneBytes snapa,
+                                                     const LaneNp np,
+                                                     const uint8_t *__restrict__ optab, int s,
+                                                     int e, int m, uint32_t len) {
+    int o0 = 0, o1 = 0, sa = 0, sb = 0, wo = 0, nc = 0;
+    uint32_t dir = 16;
+    for (uint64_t ops = rcls; ops != 0; ops >>= 8) {
+      const uint32_t c = ops & 15;
+      const int r = static_cast<int>((ops >> 4) & 15) + 1;
+      if (c == kInc0) o0 += r;
+      else if (c == kDec0) o0 -= r;
+      else if (c == kInc1) o1 += r;
+      else if (c == kDec1) o1 -= r;
+      else if (dir == 16 || c == dir) {  // (a copy of the other direction changes nothing)
+        dir = c;
+        if (nc == 0) sa = c == kCopy01 ? o0 : o1;
+        else sb = c == kCopy01 ? o0 : o1;
+        wo = c == kCopy01 ? o1 : o0;
+        nc++;
+      }
+    }
+    const bool to1 = dir == kCopy01;
+    const int w = ((to1 ? h1 : h0) + wo) & (kPair - 1);
+    if (w >= s && w <= e) return -1;
+    const int ds = to1 ? o0 : o1;  // the source head's net move
+    const uint32_t lim = (kStepLimit - i) / len;  // whole iterations left, >= 1
+    const uint32_t w_old = t.get(w);
+    uint32_t cur = w_old, k = 0;
+    bool found = false;
+    int pa = (to1 ? h0 : h1) + sa, pb = (to1 ? h0 : h1) + sb, pt = h0 + o0;
+    while (k < lim) {
+      if (k == 257) {
+        k += (lim - k) / kPair * kPair;
+        if (k >= lim) break;
+      }
+      const int a = pa & (kPair - 1);
+      if (a != w) cur = t.get(a);
+      if (nc == 2) {
+        const int b = pb & (kPair - 1);
+        if (b != w) cur = t.get(b);
+      }
+      const int tp = pt & (kPair - 1);
+      const uint32_t tv = tp == w ? cur : t.get(tp);
+      k++;
+      if ((tv & kNullMask) == 0) {
+        found = true;
+        break;
+      }
+      pa += ds;
+      pb += ds;
+      pt += o0;
+    }
+    h0 = (h0 + static_cast<int>(k) * o0) & (kPair - 1);
+    h1 = (h1 + static_cast<int>(k) * o1) & (kPair - 1);
+    i += k * len;
+    nskip += k * (len - 1 - static_cast<uint32_t>(m));
+    used0 = used1 = true;
+    write_fast(t, snapa, np, optab, w, w_old, cur);
+    v0 = t.get(h0);
+    v1 = t.get(h1);
+    if (found) {  // the k-th ']' falls through
+      rpk = 0;
+      pc = e + 1;
+      if (pc >= kPair || i >= kStepLimit) return 1;
+      nxt = np.get(pc);
+      return 0;
+    }
+    pc = s + 1;
+    return i >= kStepLimit ? 1 : 0;
+  }
+
   // One step of a replayed loop: the next body command, or the closing ']'.
   __host__ __device__ __forceinline__ bool step_replay(const LaneBytes t, const LaneBytes snapa,
                                                        const LaneNp np,
@@ -655,6 +773,12 @@ struct BffMachine {
     if (rpk & kFixedTest) {
       const int r = fixed_loop(t, snapa, np, optab, s, e, m, len);
       if (r >= 0) return r == 1;
+    }
+    if constexpr (kLogic != kLogicSelfmove) {
+      if (rpk & kCopySweep) {
+        const int r = copy_sweep(t, snapa, np, optab, s, e, m, len);
+        if (r >= 0) return r == 1;
+      }
     }
     // Up to kReplayBatch iterations.
     for (int it = 0; it < kReplayBatch; it++) {

@@ -112,7 +112,11 @@ int cubff_soup::ensure_buffers() {
     CUBFF_CUDA_TRY(cudaMalloc(&d_mutmask, size_t(batch) * (p.num_programs / 2) * sizeof(uint4)));
     CUBFF_CUDA_TRY(cudaMalloc(&d_inv, size_t(batch) * p.num_programs * sizeof(uint32_t)));
     CUBFF_CUDA_TRY(cudaMalloc(&d_readycnt, size_t(batch) * (p.num_programs / 2) * sizeof(uint32_t)));
-    CUBFF_CUDA_TRY(cudaMemset(d_readycnt, 0, size_t(batch) * (p.num_programs / 2) * sizeof(uint32_t)));
+    // On the engine's stream, which every pipelined launch follows (the
+    // legacy default stream would not order it before them).
+    CUBFF_CUDA_TRY(cudaMemsetAsync(d_readycnt, 0,
+                                   size_t(batch) * (p.num_programs / 2) * sizeof(uint32_t),
+                                   eng->stream));
     perm_first = 0;
     perm_count = 0;
   }

@@ -60,9 +60,11 @@ __global__ void mutation_mask_kernel(uint64_t s0, uint64_t e0, uint64_t npairs, 
 }
 
 constexpr int kCountSlots = kPipeCountSlots;  // per-epoch counter slots (spread the atomics)
-constexpr int kStepsPerVisit = 8;
-constexpr int kStepsLong = 256;
-constexpr uint32_t kLongRaw = 256;
+// Interpreter steps a running lane takes per iteration of its warp.  The same
+// count for every lane: an iteration lasts as long as its busiest lane, so a
+// lane given more steps than its warp-mates holds them all (and the pairs
+// they would finish and notify) for its extra steps.
+constexpr int kStepsPerVisit = 64;
 
 // Ready-queue dataflow over one or more soups.  A pair of epoch e+1 can run
 // once the two pairs of epoch e that wrote its programs are done.  A finished
@@ -279,10 +281,14 @@ __device__ __forceinline__ bool iterate(const PipeCtx &b, const PipeQueue &q, La
     // 5. A few interpreter steps; on the end, write back and notify.
     progressed = true;
     bool fin = !ln.evaluated;
-    // Pairs that have run long are the ones later epochs wait on: give them
-    // more steps per visit of the warp.
-    const int steps = m.raw() > kLongRaw ? kStepsLong : kStepsPerVisit;
-    for (int r = 0; r < steps && !fin; r++) fin = m.step(t, stk, np, optab);
+    if constexpr (L == kBffSelfmove) {
+      // bff_selfmove keeps the earlier schedule: 8 steps per visit, 256 once
+      // a pair has run 256 raw steps.
+      const int steps = m.raw() > 256 ? 256 : 8;
+      for (int r = 0; r < steps && !fin; r++) fin = m.step(t, stk, np, optab);
+    } else {
+      for (int r = 0; r < kStepsPerVisit && !fin; r++) fin = m.step(t, stk, np, optab);
+    }
     if (fin) {
       const PipeSoup &sp = b.soups[ln.si];
       if (ln.dirty || (ln.evaluated && m.mods() != 0)) {
