@@ -350,7 +350,7 @@ def cpu_sample(budget_s: float = 15.0, max_epochs: int = 10**9):
 DRAW_OPS = 21  # 32-bit integer ops of one SplitMix64 mutation draw + its threshold test
 # DRAM traffic of one 64-epoch pipelined launch of this workload (2^17 programs), from an ncu
 # capture: dram__bytes_read.sum + dram__bytes_write.sum = 175.4 MB + 24.7 MB.
-NCU_DRAM_BYTES_PER_LAUNCH = 200.2e6
+NCU_DRAM_BYTES_PER_LAUNCH = 199.1e6
 
 
 def roofline(gv, peaks, peaks_src, sm_mhz):
