@@ -45,24 +45,59 @@ SEED = 1
 MUT = 1 << 18
 K_LANG = {"bff_noheads": 8, "bff": 8, "forth": 10, "subleq": 12, "rsubleq4": 14}
 METRIC = "interp steps/s (reference-counted), bit-exact"
-CONFIG = {"workload": "bff_noheads 2^17 programs x 64 B, seed 1, mutation 2^-12, "
-                      "permutation pairing, 8192-step limit; one step = one epoch",
-          "language": LANG, "num_programs": N, "seed": SEED, "mutation_prob_q30": MUT,
-          "l2": "flushed (256 MiB write) between timed 64-epoch segments, outside the events; "
-                "epochs inside a segment overlap in the pipelined launch"}
+# Named workloads (--workload): language, programs, seed, default epochs.  The
+# default is the headline one; the others are the remaining shuffle-pairing
+# configurations of the same benchmark set, for per-language numbers.
+WORKLOADS = {
+    "bff_noheads-2^17": ("bff_noheads", 1 << 17, 1, 2048),
+    "bff-2^17": ("bff", 1 << 17, 1, 2048),
+    "bff_noheads-2^15": ("bff_noheads", 1 << 15, 0, 256),
+    "forth-2^17": ("forth", 1 << 17, 2, 4096),
+    "subleq-2^17": ("subleq", 1 << 17, 2, 4096),
+    "rsubleq4-2^17": ("rsubleq4", 1 << 17, 2, 4096),
+}
+
+
+def _log2(n: int) -> str:
+    return "2^%d" % (n.bit_length() - 1) if n & (n - 1) == 0 else str(n)
+
+
+def make_config():
+    return {"workload": f"{LANG} {_log2(N)} programs x 64 B, seed {SEED}, mutation 2^-12, "
+                        "permutation pairing, 8192-step limit; one step = one epoch",
+            "language": LANG, "num_programs": N, "seed": SEED, "mutation_prob_q30": MUT,
+            "l2": "flushed (256 MiB write) between timed 64-epoch segments, outside the events; "
+                  "epochs inside a segment overlap in the pipelined launch"}
+
+
+CONFIG = make_config()
+
+
+def set_workload(name: str) -> int:
+    """Selects a named workload; returns its default epoch count."""
+    global LANG, N, SEED, CONFIG
+    LANG, N, SEED, epochs = WORKLOADS[name]
+    CONFIG = make_config()
+    return epochs
 
 
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=2048)
+    ap.add_argument("--steps", type=int, default=None,
+                    help="epochs timed (default: the workload's, 2048 for the headline one)")
+    ap.add_argument("--workload", default="bff_noheads-2^17", choices=sorted(WORKLOADS))
     ap.add_argument("--warmup", type=int, default=8)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batch", action="store_true")
     ap.add_argument("--no-serving", action="store_true")
     ap.add_argument("--serving-jobs", type=int, default=200)
-    return ap.parse_args()
+    args = ap.parse_args()
+    epochs = set_workload(args.workload)
+    if args.steps is None:
+        args.steps = epochs
+    return args
 
 
 
@@ -343,7 +378,7 @@ def cpu_sample(budget_s: float = 15.0, max_epochs: int = 10**9):
         t_used = time.perf_counter() - t0
         ops_total, epochs_run = st["ops"], st["ep"]
     return {"value": ops_total / t_used, "unit": "steps/s", "cores": cores, "kind": kind,
-            "sample": f"{LANG} 2^17 programs seed 1, epochs 0..{epochs_run - 1} "
+            "sample": f"{LANG} {_log2(N)} programs seed {SEED}, epochs 0..{epochs_run - 1} "
                       f"({t_used:.1f} s, callback per epoch)"}
 
 
@@ -376,7 +411,7 @@ def roofline(gv, peaks, peaks_src, sm_mhz):
     achieved = work / kern_s / 1e12
     return {"bound": "int_issue", "achieved": achieved, "peak": peak, "unit": "Tintop/s",
             "frac": achieved / peak,
-            "traffic": NCU_DRAM_BYTES_PER_LAUNCH if N == 1 << 17 else None,
+            "traffic": NCU_DRAM_BYTES_PER_LAUNCH if (LANG, N) == ("bff_noheads", 1 << 17) else None,
             "traffic_unit": "bytes per 64-epoch launch (ncu capture)",
             "algorithmic_bytes_per_launch": 264.0 * (N // 2) * 64,
             "peak_source": f"{sms} SMs x 128 x {clk:.0f} MHz ({peaks_src} sm_max_mhz)",
