@@ -418,7 +418,14 @@ def roofline(gv, peaks, peaks_src, sm_mhz):
             "work_per_launch_Tintop": work / len(gv["kern_ms"]) / 1e12,
             "launch_mean_ms": kern_s * 1e3 / len(gv["kern_ms"]),
             "epochs_per_launch": epochs / len(gv["kern_ms"]),
-            "hbm_gbs_secondary": 264.0 * (N // 2) * epochs / kern_s / 1e9}
+            "hbm_gbs_secondary": 264.0 * (N // 2) * epochs / kern_s / 1e9,
+            # The same launches against the measured HBM copy bandwidth
+            # (algorithmic bytes: 264 B per pair-epoch): the memory side is
+            # far from binding.
+            "hbm": {"bound": "hbm", "achieved": 264.0 * (N // 2) * epochs / kern_s / 1e9,
+                    "peak": float(peaks.get("hbm_gbs", 6800.0)), "unit": "GB/s",
+                    "frac": 264.0 * (N // 2) * epochs / kern_s / 1e9 / float(peaks.get("hbm_gbs", 6800.0)),
+                    "peak_source": f"MEASURED_PEAKS.json hbm_gbs ({peaks_src})"}}
 
 
 def main():
