@@ -55,7 +55,11 @@ WORKLOADS = {
     "forth-2^17": ("forth", 1 << 17, 2, 4096),
     "subleq-2^17": ("subleq", 1 << 17, 2, 4096),
     "rsubleq4-2^17": ("rsubleq4", 1 << 17, 2, 4096),
+    # 2-D pairing: the 512 x 256 grid, radius 2 (pairings built on the host).
+    "bff_noheads-grid512x256": ("bff_noheads", 512 * 256, 2, 4096),
 }
+GRID = {"bff_noheads-grid512x256": (512, 256)}
+PATTERN = None  # (width, height) of the grid of the selected workload, if any
 
 
 def _log2(n: int) -> str:
@@ -63,8 +67,10 @@ def _log2(n: int) -> str:
 
 
 def make_config():
+    pairing = ("permutation pairing" if PATTERN is None else
+               f"2-D pairing on a {PATTERN[0]} x {PATTERN[1]} grid, radius 2")
     return {"workload": f"{LANG} {_log2(N)} programs x 64 B, seed {SEED}, mutation 2^-12, "
-                        "permutation pairing, 8192-step limit; one step = one epoch",
+                        f"{pairing}, 8192-step limit; one step = one epoch",
             "language": LANG, "num_programs": N, "seed": SEED, "mutation_prob_q30": MUT,
             "l2": "flushed (256 MiB write) between timed 64-epoch segments, outside the events; "
                   "epochs inside a segment overlap in the pipelined launch"}
@@ -75,8 +81,9 @@ CONFIG = make_config()
 
 def set_workload(name: str) -> int:
     """Selects a named workload; returns its default epoch count."""
-    global LANG, N, SEED, CONFIG
+    global LANG, N, SEED, CONFIG, PATTERN
     LANG, N, SEED, epochs = WORKLOADS[name]
+    PATTERN = GRID.get(name)
     CONFIG = make_config()
     return epochs
 
@@ -229,6 +236,59 @@ def gpu_value(torch, abi, steps: int, warmup: int, sm_mhz_hint: float, seed: int
             "raw": raw, "soup": soup.cpu().numpy(), "launches": launches["n"], "segments": len(ev)}
 
 
+_GRID_CACHE = {}
+
+
+def pairing_kw():
+    from cubff_gb300 import abi
+    return {} if PATTERN is None else {"pairing": abi.PAIR_PATTERN}
+
+
+def set_pattern(soup):
+    """Gives a soup of the grid workload its interaction lists."""
+    if PATTERN is None:
+        return
+    from cubff_gb300.workloads import grid_pattern
+    if PATTERN not in _GRID_CACHE:
+        _GRID_CACHE[PATTERN] = grid_pattern(*PATTERN)
+    soup.set_pattern(*_GRID_CACHE[PATTERN])
+
+
+def gpu_soup_value(torch, abi, steps: int, warmup: int, seed: int = SEED, group=None):
+    """The epochs of a workload whose pairings are built on the host (2-D
+    pairing) through the soup-level C ABI with the soup resident: warm-up
+    epochs on a scratch soup, then cubff_soup_run over the timed epochs,
+    synchronised on both sides (wall clock: the host pairing is part of the
+    epoch step, as in the reference)."""
+    import numpy as np
+    eng = abi.Engine(0)
+    w = abi.Soup(eng, LANG, N, seed, MUT, **pairing_kw())
+    set_pattern(w)
+    w.run(max(warmup, 1))
+    w.close()
+    soup = abi.Soup(eng, LANG, N, seed, MUT, **pairing_kw())
+    set_pattern(soup)
+    init = soup.read()
+    soup.run(1)
+    soup.set_epoch(0, 1)
+    soup.write(init.tobytes())
+    ops = np.zeros(steps, dtype=np.uint64)
+    raw = np.zeros(steps, dtype=np.uint64)
+    torch.cuda.synchronize()
+    replicas.barrier(group)
+    t0 = time.perf_counter()
+    abi.check(abi.lib().cubff_soup_run(soup.h, steps, ops.ctypes.data, raw.ctypes.data, None, None))
+    torch.cuda.synchronize()
+    dt = time.perf_counter() - t0
+    replicas.barrier(group)
+    out = soup.read()
+    soup.close()
+    eng.close()
+    segs = (steps + 63) // 64
+    return {"total_s": dt, "seg_ms": [dt * 1e3 / segs] * segs, "kern_ms": [dt * 1e3 / segs] * segs,
+            "ops": ops, "raw": raw, "soup": out, "launches": 4 * segs, "segments": segs}
+
+
 def gpu_e2e(torch, abi, steps: int, seed: int = SEED, group=None):
     """The same epochs through the soup-level C ABI with host buffers:
     H2D of the initial soup, cubff_soup_run (per-epoch op counts back to the
@@ -239,7 +299,8 @@ def gpu_e2e(torch, abi, steps: int, seed: int = SEED, group=None):
     init = torch.from_numpy(ref.read()).pin_memory()
     ref.close()
     out = torch.empty(N * 64, dtype=torch.uint8).pin_memory()
-    soup = abi.Soup(eng, LANG, N, seed, MUT)
+    soup = abi.Soup(eng, LANG, N, seed, MUT, **pairing_kw())
+    set_pattern(soup)
     soup.run(1)  # allocate the pairing buffers outside the timed region
     soup.set_epoch(0, 1)
     ops = np.zeros(steps, dtype=np.uint64)
@@ -353,7 +414,7 @@ def cpu_sample(budget_s: float = 15.0, max_epochs: int = 10**9):
     finally:
         if ref_dir in sys.path:
             sys.path.remove(ref_dir)
-    if refmod is not None:
+    if refmod is not None and PATTERN is None:
         p = refmod.SimulationParams()
         p.num_programs, p.seed, p.mutation_prob, p.callback_interval = N, SEED, MUT, 1
         st = {"t0": time.perf_counter(), "ops": 0, "ep": 0}
@@ -366,6 +427,7 @@ def cpu_sample(budget_s: float = 15.0, max_epochs: int = 10**9):
         ops_total, epochs_run = st["ops"], st["ep"]
     else:
         from oracle import oracle as O
+        kind = "port"
         O.build()
         t0 = time.perf_counter()
         st = {"ops": 0, "ep": 0}
@@ -374,7 +436,12 @@ def cpu_sample(budget_s: float = 15.0, max_epochs: int = 10**9):
             st["ops"] += o
             st["ep"] = e
             return (time.perf_counter() - t0 > budget_s) or e >= max_epochs
-        O.OracleSim(LANG, N, SEED, MUT).run(cb)
+        if PATTERN is None:
+            O.OracleSim(LANG, N, SEED, MUT).run(cb)
+        else:
+            from cubff_gb300.workloads import grid_pattern
+            O.OracleSim(LANG, N, SEED, MUT, pairing=O.PAIR_PATTERN,
+                        pattern=grid_pattern(*PATTERN)).run(cb)
         t_used = time.perf_counter() - t0
         ops_total, epochs_run = st["ops"], st["ep"]
     return {"value": ops_total / t_used, "unit": "steps/s", "cores": cores, "kind": kind,
@@ -454,8 +521,11 @@ def main():
     abi.lib()
     peaks, src = measured_peaks()
     with ClockSampler(local) as clocks:
-        gv = gpu_value(torch, abi, args.steps, args.warmup, peaks.get("sm_max_mhz", 2070.0),
-                       seed, group)
+        if PATTERN is None:
+            gv = gpu_value(torch, abi, args.steps, args.warmup, peaks.get("sm_max_mhz", 2070.0),
+                           seed, group)
+        else:
+            gv = gpu_soup_value(torch, abi, args.steps, args.warmup, seed, group)
     ck = clocks.summary()
     e2 = gpu_e2e(torch, abi, args.steps, seed, group)
     assert np.array_equal(gv["ops"], e2["ops"]) and np.array_equal(gv["soup"], e2["soup"]), \

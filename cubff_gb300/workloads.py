@@ -80,3 +80,27 @@ def soup_bytes(spec: SoupSpec) -> int:
 
 def log2(x: float) -> float:
     return math.log2(x)
+
+
+def grid_pattern(width: int, height: int, radius: int = 2):
+    """Interaction lists (CSR: offsets, targets) of a width x height grid of
+    programs, program i * width + j pairing with every other cell within
+    Chebyshev distance `radius`, listed cell by cell in row-major order and,
+    within a cell, in row-major (di, dj) order: the lists the reference's
+    pattern generator writes (make_2d_pattern.py:17-29), here for
+    cubff_soup_set_pattern."""
+    d = np.arange(-radius, radius + 1)
+    di = np.repeat(d, d.size)
+    dj = np.tile(d, d.size)
+    keep = (di != 0) | (dj != 0)
+    di, dj = di[keep], dj[keep]
+    i = np.arange(height)[:, None, None]
+    j = np.arange(width)[None, :, None]
+    ii, jj = i + di[None, None, :], j + dj[None, None, :]
+    valid = (ii >= 0) & (ii < height) & (jj >= 0) & (jj < width)
+    tgt = ii * width + jj
+    counts = valid.reshape(height * width, -1).sum(axis=1)
+    offs = np.zeros(height * width + 1, dtype=np.uint32)
+    np.cumsum(counts, out=offs[1:])
+    tgts = tgt.reshape(height * width, -1)[valid.reshape(height * width, -1)].astype(np.uint32)
+    return offs, tgts
