@@ -86,7 +86,11 @@ constexpr int kStepsPerVisit = 64;
 // registers read back in a later iteration.  Lane states:
 //   idle -> slot (wait for the entry) -> index -> stage -> run -> notify -> idle
 // and `exhausted` once a claim falls past the queue's last task.
-constexpr int kClaimMin = 8;
+// A warp with running lanes claims new slots only once at least kClaimMin of
+// its lanes are idle (an idle warp claims at once): a slot held by a busy
+// warp is polled only between its long iterations, so claims are left to
+// warps with many free lanes.  Swept 4-32 on the single soup and the mix.
+constexpr int kClaimMin = 20;
 
 __device__ __forceinline__ uint32_t atom_add_acq_rel(uint32_t *p, uint32_t v) {
   uint32_t old;
