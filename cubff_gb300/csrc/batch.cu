@@ -290,6 +290,15 @@ int run_soups(cubff_engine *eng, cubff_soup *const *soups, int n_soups, uint64_t
       pb.error = reinterpret_cast<int *>(eng->d_ctl + 4 * gi + 2);
       CUBFF_CUDA_TRY(cudaMemsetAsync(q.ctl, 0, 2 * sizeof(uint32_t), g.st));  // head, tail
       CUBFF_TRY(launch_pipeline(pb, pairs, eng->lanes_per_pair64, eng->device, g.st));
+      // Pattern pairings are built on the host: build the next batch of a
+      // soup whose run goes on past its cached one while this launch runs.
+      for (int i : g.members) {
+        cubff_soup *s = soups[i];
+        if (s->p.pairing != CUBFF_PAIR_PATTERN || pr[i].seg == 0) continue;
+        const uint64_t next = s->perm_first + s->perm_count, end = s->epoch + n_epochs;
+        if (next < end && !(s->pat_worker.joinable() && s->pat_pf_first == next))
+          CUBFF_TRY(s->prefetch_pattern(next, static_cast<uint32_t>(std::min<uint64_t>(s->batch, end - next))));
+      }
       for (int i : g.members) {
         cubff_soup *s = soups[i];
         Progress &p = pr[i];

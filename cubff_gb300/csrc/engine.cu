@@ -131,7 +131,13 @@ void cubff_soup::release() {
   if (d_scratch) cudaFree(d_scratch);
   if (d_counters) cudaFree(d_counters);
   if (h_counters) cudaFreeHost(h_counters);
+  drop_pattern_prefetch();
   if (h_pat_perm) cudaFreeHost(h_pat_perm);
+  if (h_pat_perm2) cudaFreeHost(h_pat_perm2);
+  if (pat_up) cudaEventDestroy(pat_up);
+  if (pat_up2) cudaEventDestroy(pat_up2);
+  h_pat_perm2 = nullptr;
+  pat_up = pat_up2 = nullptr;
   if (d_inv) cudaFree(d_inv);
   if (d_readycnt) cudaFree(d_readycnt);
   d_inv = d_readycnt = nullptr;
@@ -164,29 +170,32 @@ int cubff_soup::fill_pairing(uint64_t first, uint32_t count, cudaStream_t st) {
         return set_error(CUBFF_EINVAL, "pattern pairing without interaction lists");
       if (!h_pat_perm) {
         CUBFF_CUDA_TRY(cudaMallocHost(&h_pat_perm, (size_t(batch) * n + batch) * sizeof(uint64_t)));
+        CUBFF_CUDA_TRY(cudaEventCreateWithFlags(&pat_up, cudaEventDisableTiming));
       }
-      // The previous batch's upload must have finished before the buffer is
-      // rewritten.
-      CUBFF_CUDA_TRY(cudaStreamSynchronize(st));
+      bool have = false;
+      if (pat_worker.joinable()) {  // built ahead while the previous batch ran
+        pat_worker.join();
+        if (pat_pf_ok && pat_pf_first == first && pat_pf_count == count) {
+          std::swap(h_pat_perm, h_pat_perm2);
+          std::swap(pat_up, pat_up2);
+          have = true;
+        }
+        pat_pf_count = 0;
+      }
+      if (!have) {
+        // The last upload from this buffer must have finished before it is
+        // rewritten.
+        CUBFF_CUDA_TRY(cudaEventSynchronize(pat_up));
+        compute_pattern(first, count, h_pat_perm);
+      }
       uint32_t *hp = reinterpret_cast<uint32_t *>(h_pat_perm);
       uint64_t *hn = h_pat_perm + (size_t(batch) * n + 1) / 2;
-      const unsigned hw = std::max(1u, std::min<unsigned>(std::thread::hardware_concurrency(), count));
-      std::vector<std::thread> pool;
-      for (unsigned w = 0; w < hw; w++) {
-        pool.emplace_back([&, w] {
-          std::vector<uint32_t> order;
-          std::vector<uint8_t> used;
-          for (uint32_t e = w; e < count; e += hw)
-            hn[e] = pattern_pairing_host(s0, first + e, n, pat_offs.data(), pat_tgts.data(),
-                                         hp + size_t(e) * n, order, used);
-        });
-      }
-      for (auto &t : pool) t.join();
       pat_ni.assign(hn, hn + count);
       CUBFF_CUDA_TRY(cudaMemcpyAsync(d_perm, hp, size_t(count) * n * sizeof(uint32_t),
                                      cudaMemcpyHostToDevice, st));
       CUBFF_CUDA_TRY(cudaMemcpyAsync(d_num_indices, hn, size_t(count) * sizeof(uint64_t),
                                      cudaMemcpyHostToDevice, st));
+      CUBFF_CUDA_TRY(cudaEventRecord(pat_up, st));
       break;
     }
     default:
@@ -197,6 +206,55 @@ int cubff_soup::fill_pairing(uint64_t first, uint32_t count, cudaStream_t st) {
   perm_first = first;
   perm_count = count;
   return CUBFF_OK;
+}
+
+// Pattern pairings of epochs [first, first + count) into a staging buffer
+// (batch * n shuffle entries, then the epochs' num_indices), on host threads.
+void cubff_soup::compute_pattern(uint64_t first, uint32_t count, uint64_t *buf) {
+  const uint64_t n = p.num_programs;
+  uint32_t *hp = reinterpret_cast<uint32_t *>(buf);
+  uint64_t *hn = buf + (size_t(batch) * n + 1) / 2;
+  const unsigned hw = std::max(1u, std::min<unsigned>(std::thread::hardware_concurrency(), count));
+  std::vector<std::thread> pool;
+  for (unsigned w = 0; w < hw; w++) {
+    pool.emplace_back([&, w] {
+      std::vector<uint32_t> order;
+      std::vector<uint8_t> used;
+      for (uint32_t e = w; e < count; e += hw)
+        hn[e] = pattern_pairing_host(s0, first + e, n, pat_offs.data(), pat_tgts.data(),
+                                     hp + size_t(e) * n, order, used);
+    });
+  }
+  for (auto &t : pool) t.join();
+}
+
+// Starts building the pattern pairings of [first, first + count) on a host
+// thread, into the second staging buffer once its last upload has finished;
+// fill_pairing takes them when it gets to `first`.
+int cubff_soup::prefetch_pattern(uint64_t first, uint32_t count) {
+  drop_pattern_prefetch();
+  const uint64_t n = p.num_programs;
+  if (!h_pat_perm2) {
+    CUBFF_CUDA_TRY(cudaMallocHost(&h_pat_perm2, (size_t(batch) * n + batch) * sizeof(uint64_t)));
+    CUBFF_CUDA_TRY(cudaEventCreateWithFlags(&pat_up2, cudaEventDisableTiming));
+  }
+  pat_pf_first = first;
+  pat_pf_count = count;
+  pat_pf_ok = false;
+  const int device = eng->device;
+  pat_worker = std::thread([this, first, count, device] {
+    cudaSetDevice(device);
+    if (cudaEventSynchronize(pat_up2) != cudaSuccess) return;
+    compute_pattern(first, count, h_pat_perm2);
+    pat_pf_ok = true;
+  });
+  return CUBFF_OK;
+}
+
+void cubff_soup::drop_pattern_prefetch() {
+  if (pat_worker.joinable()) pat_worker.join();
+  pat_pf_count = 0;
+  pat_pf_ok = false;
 }
 
 int cubff_soup::apply_reset(cudaStream_t st) {
@@ -399,6 +457,7 @@ int cubff_soup_set_pattern(cubff_soup *soup, const uint32_t *offs, const uint32_
                          static_cast<unsigned long long>(i));
     }
   }
+  soup->drop_pattern_prefetch();  // built from the previous lists
   soup->pat_offs.assign(offs, offs + n + 1);
   soup->pat_tgts.assign(tgts, tgts + ne);
   soup->perm_count = 0;  // cached pairings are stale

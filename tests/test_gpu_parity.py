@@ -211,3 +211,53 @@ def test_run_epochs_kernel_matches_oracle(lang):
     got_ops = _host(counts).reshape(E, 2)[:, 0].tolist()
     assert got_ops == want_ops
     assert np.array_equal(_host(d_soup), want)
+
+
+@pytest.mark.parametrize("lang,w,h,epochs", [("bff_noheads", 64, 32, 200), ("forth", 32, 32, 150)])
+def test_pattern_run_across_batches_matches_oracle(lang, w, h, epochs):
+    """One soup_run call spanning several 64-epoch batches of 2-D pairings:
+    the host builds each next batch while the previous one runs."""
+    n = w * h
+    offs, tgts = O.grid_pattern(w, h, 2)
+    soup = abi.Soup(harness.engine(), lang, n, 5, 1 << 18, abi.PAIR_PATTERN)
+    soup.set_pattern(offs, tgts)
+    ops, _raw = soup.run(epochs)
+    got = soup.read()
+    soup.close()
+    want_ops, want = [], {}
+
+    def cb(e, s, o, r):
+        want_ops.append(o)
+        if e == epochs:
+            want["soup"] = s.copy()
+        return e >= epochs
+    O.OracleSim(lang, n, 5, 1 << 18, pairing=O.PAIR_PATTERN, pattern=(offs, tgts)).run(cb)
+    assert [int(x) for x in ops] == want_ops
+    assert np.array_equal(got, want["soup"])
+
+
+def test_pattern_batch_run_across_batches_matches_oracle():
+    """Two pattern soups advanced together by cubff_batch_run over 140 epochs."""
+    specs = [(64, 32, 7), (32, 16, 8)]
+    soups, csrs = [], []
+    for w, h, seed in specs:
+        csr = O.grid_pattern(w, h, 2)
+        s = abi.Soup(harness.engine(), "bff_noheads", w * h, seed, 1 << 18, abi.PAIR_PATTERN)
+        s.set_pattern(*csr)
+        soups.append(s)
+        csrs.append(csr)
+    ops = abi.batch_run(harness.engine(), soups, 140)
+    got = [s.read() for s in soups]
+    for s in soups:
+        s.close()
+    for (w, h, seed), csr, o, g in zip(specs, csrs, ops, got):
+        want_ops, want = [], {}
+
+        def cb(e, s, oo, r):
+            want_ops.append(oo)
+            if e == 140:
+                want["soup"] = s.copy()
+            return e >= 140
+        O.OracleSim("bff_noheads", w * h, seed, 1 << 18, pairing=O.PAIR_PATTERN, pattern=csr).run(cb)
+        assert [int(x) for x in o] == want_ops
+        assert np.array_equal(g, want["soup"])
