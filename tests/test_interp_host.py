@@ -108,6 +108,13 @@ CRAFTED = {
                     # fixed tests: the ']' reads a byte the body never changes
                     b"+[<+>]", b"+[<<+>-<<+>>>]" + b"q" * 4, b"+[>+<]", b"+[>>++<<}]",
                     b"+[<" + b"q" * 20 + b"---}>]", b"-[<+<+>>]" + b"+" * 30,
+                    # copy sweeps: every iteration writes one byte from a sweeping head
+                    # (also reading the written byte, and running to the step limit)
+                    b"+[<.]", b"+[<.]" + b"q" * 40 + b"\x00" + b"q" * 20, b"+[>.]" + b"q" * 70,
+                    b"+[<<<.]", b"+[.<]", b"+[<.<.]", b"+[.,<]", b"+[,.>>]" + b"q" * 9,
+                    b"+[" + b"q" * 9 + b"<" + b"q" * 5 + b"." + b"q" * 3 + b"]",
+                    b"}}}}}}+[<.]" + b"q" * 30, b"+[}}},{{{]", b"+[},]" + b"\x00" * 3 + b"q" * 5,
+                    b">>>>+[<<<<<<.>>>>>]",
                     # a tape that ran 6241 loop iterations of an h1-drift loop
                     bytes.fromhex(
                         "515b7d7b7b7d7d7b807d7d197b7d7d7b7b7d7d7b7b7d7d7b7b7dba7b7b7d7d7b7b7d7d"
