@@ -1,6 +1,6 @@
 /* cubff_oracle.h — CPU oracle for the cubff epoch step (mutate -> pair -> run
  * -> split).  TEST INFRASTRUCTURE ONLY: tests, the smoke check and the CPU
- * baseline leg of the benchmark call it as the checker.  The product (the
+ * baseline leg of the benchmark call it to compare against.  The product (the
  * cubff_gb300 package) never links or calls it.
  *
  * Every function restates the reference algorithm from its semantics; each

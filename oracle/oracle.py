@@ -2,7 +2,7 @@
 epoch step).
 
 TEST INFRASTRUCTURE ONLY.  Imported by tests/, by ``__graft_entry__.smoke()``
-and by the CPU-baseline leg of ``bench.py`` as the checker; the product package
+and by the CPU-baseline leg of ``bench.py``, to compare against; the product package
 ``cubff_gb300`` never imports it.
 
 ``OracleSim.run`` mirrors the epoch loop of ``Simulation<L>::RunSimulation``
