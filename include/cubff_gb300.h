@@ -166,7 +166,11 @@ int cubff_soup_destroy(cubff_soup *soup);
 
 /* allowed_interactions in CSR form (program i may pair with
  * tgts[offs[i] .. offs[i+1])), for CUBFF_PAIR_PATTERN.  offs has
- * num_programs+1 entries.  Self-pairs (i listed for i) are rejected. */
+ * num_programs+1 entries.  Self-pairs (i listed for i) are rejected.  The
+ * lists are copied.  Pattern pairings are built on host threads, a batch of
+ * up to 64 epochs at a time (as the reference builds them on the host); a
+ * run longer than one batch builds the next batch while the current one
+ * runs on the device. */
 int cubff_soup_set_pattern(cubff_soup *soup, const uint32_t *offs,
                            const uint32_t *tgts);
 
