@@ -50,6 +50,7 @@ SIGNATURES = {
     "cubff_run_epochs_workspace_bytes": (sz, [u64, u32]),
     "cubff_run_epochs": (ci, [ci, vp, vp, vp, u64, u64, u32, u32, u64, vp, vp, sz, vp]),
     "cubff_run_epochs_status": (ci, [vp, u64, u32, vp]),
+    "cubff_set_wait_limit_ns": (ci, [u64, ctypes.POINTER(u64)]),
     "cubff_engine_create": (ci, [ci, ctypes.POINTER(vp)]),
     "cubff_engine_destroy": (ci, [vp]),
     "cubff_soup_create": (ci, [vp, ctypes.POINTER(SoupParams), ctypes.POINTER(vp)]),
@@ -194,6 +195,14 @@ class Soup:
             self.close()
         except Exception:
             pass
+
+
+def set_wait_limit_ns(ns: int) -> int:
+    """Sets the bound of the waits inside pipelined launches; returns the
+    previous bound (cubff_set_wait_limit_ns)."""
+    prev = u64(0)
+    check(lib().cubff_set_wait_limit_ns(ns, ctypes.byref(prev)))
+    return int(prev.value)
 
 
 def batch_run(engine: Engine, soups, n_epochs: int) -> np.ndarray:

@@ -53,8 +53,22 @@ def _run(cmd):
     return out.stdout + out.stderr
 
 
+_ELF_MACHINE = {"x86_64": 62, "aarch64": 183}
+
+
+def _native(path) -> bool:
+    """True when the ELF file at path was built for this machine (an in-tree
+    artefact copied from another architecture is rebuilt, whatever its age)."""
+    want = _ELF_MACHINE.get(platform.machine())
+    if want is None:
+        return True
+    with open(path, "rb") as f:
+        head = f.read(20)
+    return len(head) == 20 and head[:4] == b"\x7fELF" and int.from_bytes(head[18:20], "little") == want
+
+
 def _newer(target, deps):
-    if not os.path.exists(target):
+    if not os.path.exists(target) or not _native(target):
         return False
     t = os.path.getmtime(target)
     return all(os.path.getmtime(d) <= t for d in deps)

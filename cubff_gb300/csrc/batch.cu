@@ -101,9 +101,9 @@ struct Progress {
 // groups' error flags.  The groups' streams must be idle (synchronised).
 static int read_counters(cubff_soup *const *soups, const std::vector<Group> &groups,
                          std::vector<Progress> &pr, uint64_t *const *ops, uint64_t *const *raw,
-                         const uint32_t *h_ctl, bool *timed_out) {
+                         const uint32_t *h_ctl, uint32_t *fault) {
   for (const Group &g : groups) {
-    if (h_ctl[4 * (&g - groups.data()) + 2] != 0) *timed_out = true;
+    *fault = std::max(*fault, h_ctl[4 * (&g - groups.data()) + 2]);
     for (int i : g.members) {
       const uint64_t rows = pr[i].done - pr[i].cbase;
       const unsigned long long *h = soups[i]->h_counters;
@@ -200,7 +200,7 @@ int run_soups(cubff_engine *eng, cubff_soup *const *soups, int n_soups, uint64_t
   }
 
   std::unique_ptr<PipeBatch> b(new PipeBatch);
-  bool timed_out = false;
+  uint32_t fault = 0;  // the launches' error flag: 1 a wait timed out, 2 a bad queue entry
   while (true) {
     // A soup whose counter chunk is full: read every soup's counters back.
     bool flush = false;
@@ -209,8 +209,8 @@ int run_soups(cubff_engine *eng, cubff_soup *const *soups, int n_soups, uint64_t
     if (flush) {
       CUBFF_TRY(copy_counters(soups, groups, pr, eng));
       for (const Group &g : groups) CUBFF_CUDA_TRY(cudaStreamSynchronize(g.st));
-      CUBFF_TRY(read_counters(soups, groups, pr, ops, raw, eng->h_ctl, &timed_out));
-      if (timed_out) break;
+      CUBFF_TRY(read_counters(soups, groups, pr, ops, raw, eng->h_ctl, &fault));
+      if (fault) break;
       for (const Group &g : groups) {
         for (int i : g.members) {
           pr[i].cbase = pr[i].done;
@@ -288,6 +288,7 @@ int run_soups(cubff_engine *eng, cubff_soup *const *soups, int n_soups, uint64_t
       q.n_soups = static_cast<uint32_t>(pb.n_soups);
       q.lang = g.lang;
       pb.error = reinterpret_cast<int *>(eng->d_ctl + 4 * gi + 2);
+      pb.wait_limit_ns = pipeline_wait_limit_ns();
       CUBFF_CUDA_TRY(cudaMemsetAsync(q.ctl, 0, 2 * sizeof(uint32_t), g.st));  // head, tail
       CUBFF_TRY(launch_pipeline(pb, pairs, eng->lanes_per_pair64, eng->device, g.st));
       // Pattern pairings are built on the host: build the next batch of a
@@ -314,10 +315,10 @@ int run_soups(cubff_engine *eng, cubff_soup *const *soups, int n_soups, uint64_t
     if (!any) break;
   }
 
-  if (!timed_out) {
+  if (!fault) {
     CUBFF_TRY(copy_counters(soups, groups, pr, eng));
     for (const Group &g : groups) CUBFF_CUDA_TRY(cudaStreamSynchronize(g.st));
-    CUBFF_TRY(read_counters(soups, groups, pr, ops, raw, eng->h_ctl, &timed_out));
+    CUBFF_TRY(read_counters(soups, groups, pr, ops, raw, eng->h_ctl, &fault));
   }
   if (G > 1) {
     for (size_t g = 0; g < G; g++) {
@@ -326,9 +327,12 @@ int run_soups(cubff_engine *eng, cubff_soup *const *soups, int n_soups, uint64_t
     }
   }
   for (int i = 0; i < n_soups; i++) soups[i]->epoch += pr[i].done;
-  if (timed_out) {
+  if (fault) {
     eng->dirty = true;
     for (int i = 0; i < n_soups; i++) soups[i]->dirty = true;
+    if (fault == 2)
+      return set_error(CUBFF_EDEVICE,
+                       "a ready-queue entry was out of range; the soups' state is invalid");
     return set_error(CUBFF_ETIMEDOUT,
                      "a pipelined epoch wait timed out; the soups' state is invalid");
   }

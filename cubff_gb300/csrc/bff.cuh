@@ -378,9 +378,9 @@ struct BffMachine {
   static constexpr uint32_t kScanLoop = 1u << 23;
   static constexpr uint32_t kCountLoop = 1u << 24;
   static constexpr uint32_t kFixedTest = 1u << 25;
-  // Copy sweeps (copy_sweep) are off for bff_selfmove, whose copies move h1
-  // (they are not a fixed-destination sweep), and whose pipelined kernel
-  // stays built from the code it was validated with.
+  // Copy sweeps (copy_sweep) never apply to bff_selfmove, whose copies move
+  // h1 (they are not a fixed-destination sweep): enter_replay does not flag
+  // them there.
   static constexpr uint32_t kCopySweep = 1u << 26;
   static constexpr int kReplayBatch = 8;  // replayed iterations per step call
 
@@ -505,7 +505,7 @@ struct BffMachine {
     // the other direction right after a copy writes back the byte it just
     // read: it changes nothing.
     bool sweep = !counter && !fixed;
-    if constexpr (kLogic != kLogicSelfmove) {  // (bff_selfmove: see kCopySweep)
+    if (kLogic != kLogicSelfmove) {  // (bff_selfmove: see kCopySweep)
       int o0 = 0, o1 = 0, wo = 0, nc = 0;
       uint32_t dir = 16, prev = 16;
       for (int o2 = 0; o2 < n && sweep; o2++) {
@@ -774,11 +774,9 @@ struct BffMachine {
       const int r = fixed_loop(t, snapa, np, optab, s, e, m, len);
       if (r >= 0) return r == 1;
     }
-    if constexpr (kLogic != kLogicSelfmove) {
-      if (rpk & kCopySweep) {
-        const int r = copy_sweep(t, snapa, np, optab, s, e, m, len);
-        if (r >= 0) return r == 1;
-      }
+    if (rpk & kCopySweep) {
+      const int r = copy_sweep(t, snapa, np, optab, s, e, m, len);
+      if (r >= 0) return r == 1;
     }
     // Up to kReplayBatch iterations.
     for (int it = 0; it < kReplayBatch; it++) {

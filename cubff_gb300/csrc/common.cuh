@@ -58,14 +58,18 @@ __device__ __forceinline__ uint32_t lane_base(uint32_t tid) {
 }
 
 // One thread's 128-byte tape (or 128-byte stack) in the layout above.
+// Positions are taken mod 128 (one AND), so no index a caller computes can
+// leave the thread's own 128 bytes: every interpreter keeps its positions in
+// 0..127 anyway, and the parity tests would show any position that relied on
+// the wrap.
 struct LaneBytes {
   uint8_t *s;     // dynamic shared memory block holding the layout
   uint32_t base;  // lane_base(tid)
   __host__ __device__ __forceinline__ uint32_t get(int p) const {
-    return s[base + (static_cast<uint32_t>(p) << 7)];
+    return s[base + ((static_cast<uint32_t>(p) & (kPair - 1)) << 7)];
   }
   __host__ __device__ __forceinline__ void set(int p, uint32_t v) const {
-    s[base + (static_cast<uint32_t>(p) << 7)] = static_cast<uint8_t>(v);
+    s[base + ((static_cast<uint32_t>(p) & (kPair - 1)) << 7)] = static_cast<uint8_t>(v);
   }
 };
 
@@ -78,14 +82,20 @@ constexpr int kNpSpare = 8;
 constexpr int kNpEntries = kPair + 1 + kNpSpare;
 constexpr int kNpBytes = kNpEntries * 128 * 2;
 
+// Entries are clamped to the last one (kNpEntries - 1) for the same reason:
+// the array never reaches past its thread's column.
 struct LaneNp {
   uint16_t *s;    // nullptr: no array (the interpreter stays in its basic mode)
   uint32_t base;  // tid within the 128-thread block
+  __host__ __device__ __forceinline__ static uint32_t clamp(int p) {
+    const uint32_t q = static_cast<uint32_t>(p);
+    return q < kNpEntries - 1 ? q : kNpEntries - 1;
+  }
   __host__ __device__ __forceinline__ uint32_t get(int p) const {
-    return s[base + (static_cast<uint32_t>(p) << 7)];
+    return s[base + (clamp(p) << 7)];
   }
   __host__ __device__ __forceinline__ void set(int p, uint32_t v) const {
-    s[base + (static_cast<uint32_t>(p) << 7)] = static_cast<uint16_t>(v);
+    s[base + (clamp(p) << 7)] = static_cast<uint16_t>(v);
   }
 };
 

@@ -343,6 +343,8 @@ int cubff_shuffle_indices(uint64_t params_seed, uint64_t first_epoch, uint32_t n
                           size_t scratch_bytes, void *stream) {
   if (!d_out || !d_scratch || num_programs == 0 || num_programs > 0xffffffffull)
     return set_error(CUBFF_EINVAL, "shuffle_indices: bad arguments");
+  if (shuffle_scratch_bytes(num_programs, n_epochs) == SIZE_MAX)
+    return set_error(CUBFF_EINVAL, "shuffle_indices: num_programs x n_epochs too large");
   if (scratch_bytes < shuffle_scratch_bytes(num_programs, n_epochs))
     return set_error(CUBFF_EINVAL, "shuffle_indices: scratch too small (%zu < %zu)",
                      scratch_bytes, shuffle_scratch_bytes(num_programs, n_epochs));

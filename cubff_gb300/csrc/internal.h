@@ -78,8 +78,11 @@ struct PipeBatch {
   PipeSoup soups[kMaxPipeSoups];
   PipeQueue queue;
   int n_soups;
-  int *error;                   // set when a bounded wait gives up
+  int *error;                   // 1: a bounded wait gave up; 2: a bad queue entry
+  uint64_t wait_limit_ns;       // bound of every wait inside the launch
 };
+// The wait bound given to pipelined launches (cubff_set_wait_limit_ns).
+uint64_t pipeline_wait_limit_ns();
 constexpr int kPipeCountSlots = 32;
 
 // Launchers (epoch.cu / pairing.cu / pipeline.cu).

@@ -185,8 +185,12 @@ unsigned blocks_for(uint64_t m, unsigned t) { return static_cast<unsigned>((m + 
 
 }  // namespace
 
+// Six uint32 arrays of n * n_epochs entries; SIZE_MAX when that does not fit
+// in size_t (so no scratch size can pass a check against it).
 size_t shuffle_scratch_bytes(uint64_t n, uint32_t n_epochs) {
-  return size_t(6) * n * n_epochs * sizeof(uint32_t);
+  constexpr uint64_t kPerDraw = 6 * sizeof(uint32_t);
+  if (n_epochs != 0 && n > (SIZE_MAX / kPerDraw) / n_epochs) return SIZE_MAX;
+  return size_t(kPerDraw) * n * n_epochs;
 }
 
 int launch_shuffle(uint64_t s0, uint64_t first_epoch, uint32_t E, uint64_t n,
@@ -250,7 +254,9 @@ int launch_cyclic(uint64_t first_epoch, uint32_t E, uint64_t n, uint32_t *out,
 //    exits.  Larger requests are rejected with CUBFF_EINVAL.
 //  * The first call on a device resolves the array's device address with
 //    cudaGetSymbolAddress (with that device current) and caches it; make that
-//    first call before any stream capture.
+//    first call before any stream capture.  cudaDeviceReset (or anything else
+//    that destroys the device's primary context) invalidates the cached
+//    address: do not call this entry point on that device afterwards.
 //  * All calls share the one array.  The counts the kernels accumulate are
 //    cleared at the start of every call; everything else is overwritten.
 //    Calls whose work overlaps on the GPU (different streams, or different
@@ -274,11 +280,12 @@ extern "C" int cubff_shuffle_indices_noalloc(uint64_t params_seed, uint64_t firs
   using namespace cubff;
   if (!d_out || num_programs == 0 || n_epochs == 0)
     return set_error(CUBFF_EINVAL, "shuffle_indices_noalloc: bad arguments");
-  if (num_programs * n_epochs > kNoAllocMaxDraws)
+  // Tested by division: the product itself could wrap.
+  if (num_programs > kNoAllocMaxDraws || n_epochs > kNoAllocMaxDraws / num_programs)
     return set_error(CUBFF_EINVAL,
-                     "shuffle_indices_noalloc: num_programs * n_epochs = %llu exceeds the "
+                     "shuffle_indices_noalloc: num_programs %llu x n_epochs %u exceeds the "
                      "built-in scratch limit of %llu draws",
-                     static_cast<unsigned long long>(num_programs * n_epochs),
+                     static_cast<unsigned long long>(num_programs), n_epochs,
                      static_cast<unsigned long long>(kNoAllocMaxDraws));
   int dev = 0;
   CUBFF_CUDA_TRY(cudaGetDevice(&dev));

@@ -9,12 +9,15 @@
 // independent, so a batch of soups of one language (any sizes and mutation
 // rates) shares one persistent launch and one ready queue.
 //
-// Every wait is bounded (10 s of %globaltimer); a timeout sets *error, the
-// waiting lanes give up, and the host reports CUBFF_ETIMEDOUT.  Results are
+// Every wait is bounded (10 s of %globaltimer by default); a timeout sets
+// *error = 1, the waiting lanes give up, and the host reports CUBFF_ETIMEDOUT.
+// A ready-queue entry naming no task of the launch sets *error = 2 (reported
+// as CUBFF_EDEVICE) instead of being used as an index.  Results are
 // bit-identical to the per-epoch launches: every program sees the same
 // sequence of pair operations (MutateAndRunPrograms, common_language.h:163-192)
 // with the same inputs.
 #include <algorithm>
+#include <atomic>
 
 #include "epoch_body.cuh"
 
@@ -37,7 +40,8 @@ __device__ __forceinline__ uint64_t globaltimer_ns() {
   return t;
 }
 
-constexpr uint64_t kWaitLimitNs = 10ull * 1000 * 1000 * 1000;
+constexpr uint64_t kDefaultWaitLimitNs = 10ull * 1000 * 1000 * 1000;
+std::atomic<uint64_t> g_wait_limit_ns{kDefaultWaitLimitNs};
 
 // Mutation masks of MutateAndRunPrograms (common_language.h:172-180) for
 // epochs [e0, e0 + E): bit i of mask[e][k] is set iff draw i of pair k,
@@ -119,6 +123,7 @@ struct Lane {
 struct PipeCtx {
   const PipeSoup *soups;
   int *error;
+  uint64_t wait_limit_ns;
 };
 
 // Soup of global task `task` among soups [lo, hi) (sorted by task_base).
@@ -182,7 +187,12 @@ __device__ __forceinline__ bool iterate(const PipeCtx &b, const PipeQueue &q, La
 
   if (ln.state == kSlot) {
     // 2. Waiting for the claimed slot's entry (polled in an earlier iteration).
-    if (ln.qv != 0) {
+    if (ln.qv != 0 && ln.qv - 1 >= q.total) {
+      // Only pushes of tasks of this launch fill the queue; any other value
+      // is reported (error 2) instead of being used as an index.
+      atomicExch(b.error, 2);
+      ln.state = kExhausted;
+    } else if (ln.qv != 0) {
       ln.task = ln.qv - 1;
       // Consumed: leave the entry zero for the next launch.
       q.queue[ln.slot - q.initial] = 0;
@@ -202,7 +212,7 @@ __device__ __forceinline__ bool iterate(const PipeCtx &b, const PipeQueue &q, La
         const uint64_t now = globaltimer_ns();
         if (ln.t_wait == 0) {
           ln.t_wait = now;
-        } else if (now - ln.t_wait > kWaitLimitNs) {
+        } else if (now - ln.t_wait > b.wait_limit_ns) {
           atomicExch(b.error, 1);
           ln.state = kExhausted;
         }
@@ -285,14 +295,7 @@ __device__ __forceinline__ bool iterate(const PipeCtx &b, const PipeQueue &q, La
     // 5. A few interpreter steps; on the end, write back and notify.
     progressed = true;
     bool fin = !ln.evaluated;
-    if constexpr (L == kBffSelfmove) {
-      // bff_selfmove keeps the earlier schedule: 8 steps per visit, 256 once
-      // a pair has run 256 raw steps.
-      const int steps = m.raw() > 256 ? 256 : 8;
-      for (int r = 0; r < steps && !fin; r++) fin = m.step(t, stk, np, optab);
-    } else {
-      for (int r = 0; r < kStepsPerVisit && !fin; r++) fin = m.step(t, stk, np, optab);
-    }
+    for (int r = 0; r < kStepsPerVisit && !fin; r++) fin = m.step(t, stk, np, optab);
     if (fin) {
       const PipeSoup &sp = b.soups[ln.si];
       if (ln.dirty || (ln.evaluated && m.mods() != 0)) {
@@ -418,7 +421,7 @@ __global__ void __launch_bounds__(kThreads, (L <= kBffSelfmove) ? 3 : 4)
   const LaneBytes stk{smem + kGroups * kGroupBytes, lane_base(tid)};
   const uint32_t warp = blockIdx.x * (kThreads / 32) + (tid >> 5);
   const LaneNp np{L <= kBffSelfmove ? npa : nullptr, tid};
-  const PipeCtx b{soups, pb.error};
+  const PipeCtx b{soups, pb.error, pb.wait_limit_ns};
   const PipeQueue q = pb.queue;
   serve<L>(b, q, optab, cmdflag, t, stk, np, lane, warp % kCountSlots);
 }
@@ -455,6 +458,8 @@ int launch_pipeline_t(const PipeBatch &b, uint64_t total_pairs, uint32_t lanes_p
 }
 
 }  // namespace
+
+uint64_t pipeline_wait_limit_ns() { return g_wait_limit_ns.load(); }
 
 int launch_pipeline(const PipeBatch &b, uint64_t total_pairs, uint32_t lanes_per_pair64,
                     int device, cudaStream_t stream) {
@@ -612,6 +617,7 @@ extern "C" int cubff_run_epochs(int lang, uint8_t *d_programs, const uint32_t *d
   q.lang = lang;
   b.n_soups = 1;
   b.error = reinterpret_cast<int *>(w.ctl + 2);
+  b.wait_limit_ns = pipeline_wait_limit_ns();
   CUBFF_TRY(launch_pipeline(b, P, 0, dev, st));
   reduce_counts_kernel<<<(n_epochs + 127) / 128, 128, 0, st>>>(w.counters, n_epochs, d_counts);
   CUBFF_CUDA_TRY(cudaGetLastError());
@@ -627,6 +633,15 @@ extern "C" int cubff_run_epochs_status(const void *d_workspace, uint64_t num_pro
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   CUBFF_CUDA_TRY(cudaMemcpyAsync(&err, w.ctl + 2, sizeof(int), cudaMemcpyDeviceToHost, st));
   CUBFF_CUDA_TRY(cudaStreamSynchronize(st));
+  if (err == 2) return set_error(CUBFF_EDEVICE, "run_epochs: a ready-queue entry was out of range");
   if (err) return set_error(CUBFF_ETIMEDOUT, "run_epochs: a pipelined wait timed out");
+  return CUBFF_OK;
+}
+
+extern "C" int cubff_set_wait_limit_ns(uint64_t ns, uint64_t *previous) {
+  using namespace cubff;
+  if (ns == 0) return set_error(CUBFF_EINVAL, "set_wait_limit_ns: the limit must be > 0");
+  const uint64_t old = g_wait_limit_ns.exchange(ns);
+  if (previous) *previous = old;
   return CUBFF_OK;
 }

@@ -74,6 +74,19 @@ def serving_jobs(count: int = 2000, rate_per_s: float = 20.0, seed: int = 7):
     return arrivals.tolist(), jobs
 
 
+def serving_sample(count: int = 24, max_program_epochs: int = 1 << 26,
+                   seed: int = 2024) -> List[int]:
+    """Indices of the serving jobs that are also run on the CPU: `count` jobs
+    drawn without replacement (generator keyed by `seed`) among those with
+    num_programs * epochs <= max_program_epochs, so the CPU side stays within
+    minutes per job.  Sorted."""
+    _, jobs = serving_jobs()
+    eligible = [j for j, s in enumerate(jobs) if s.num_programs * s.epochs <= max_program_epochs]
+    rng = np.random.default_rng(seed)
+    pick = rng.choice(len(eligible), size=min(count, len(eligible)), replace=False)
+    return sorted(eligible[int(i)] for i in pick)
+
+
 def soup_bytes(spec: SoupSpec) -> int:
     return spec.num_programs * 64
 

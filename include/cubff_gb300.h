@@ -125,6 +125,15 @@ int cubff_run_epochs(int lang, uint8_t *d_programs, const uint32_t *d_shuf_idx,
 int cubff_run_epochs_status(const void *d_workspace, uint64_t num_programs,
                             uint32_t n_epochs, void *stream);
 
+/* Bound of the waits inside pipelined launches (cubff_run_epochs, soup runs,
+ * batches, the server): a lane waiting longer than ns nanoseconds for a
+ * ready-queue entry sets the launch's error flag, every lane gives up, and
+ * the run returns CUBFF_ETIMEDOUT (soups touched by it are left invalid and
+ * must be reloaded or recreated).  Process-wide; applies to launches made
+ * after the call; default 10 s.  No reference counterpart (the reference's
+ * launches have no waits).  *previous (nullable) gets the old bound. */
+int cubff_set_wait_limit_ns(uint64_t ns, uint64_t *previous);
+
 /* Allocation-free variant of cubff_shuffle_indices.  It has no counterpart
  * in the reference.  It serves callers that cannot allocate device memory
  * (an application that owns the GPU's allocator, or a path that cannot take
@@ -132,8 +141,10 @@ int cubff_run_epochs_status(const void *d_workspace, uint64_t num_programs,
  * caller-provided scratch buffer it uses a fixed 6 MiB array in this
  * library's device memory, so num_programs * n_epochs must not exceed 2^18
  * (larger requests return CUBFF_EINVAL).  The first call on a device looks up
- * the array's device address (make it before any stream capture).  All calls
- * share the array, so calls that overlap on the GPU race; order them. */
+ * the array's device address (make it before any stream capture); a
+ * cudaDeviceReset of that device invalidates it, so do not call this entry
+ * point there afterwards.  All calls share the array, so calls that overlap
+ * on the GPU race; order them (e.g. on one stream). */
 int cubff_shuffle_indices_noalloc(uint64_t params_seed, uint64_t first_epoch,
                                   uint32_t n_epochs, uint64_t num_programs,
                                   uint32_t *d_out, void *stream);
@@ -226,7 +237,7 @@ uint64_t cubff_soup_footprint_bytes(const cubff_soup_params *params);
 /* ---- layer 3: batching ------------------------------------------------- */
 /* Advances every soup by n_epochs epochs, as cubff_soup_run does for each
  * (same results, soup for soup), but all soups together: soups of one
- * language share persistent pipelined launches (up to 128 soups per launch),
+ * language share persistent pipelined launches (up to 64 soups per launch),
  * and the launches of different languages run on streams of their own.
  * ops: host array [n_soups][n_epochs].  Every soup must belong to engine;
  * pattern-paired soups need their interaction lists. */

@@ -14,6 +14,13 @@ GPU tests can run without it.
 
     python tests/golden/make_golden.py            # small fixtures (~1 min)
     python tests/golden/make_golden.py long       # through-emergence pins
+    python tests/golden/make_golden.py c2         # bff, bff_noheads 2^17 to 16384 epochs
+    python tests/golden/make_golden.py c3         # forth/subleq/rsubleq4 + 512x256 grid
+    python tests/golden/make_golden.py c4         # the 64-soup batched mix, 2048 epochs
+    python tests/golden/make_golden.py c5         # a seeded sample of the serving jobs
+
+The reference tree is read from $CUBFF_REFERENCE (default: the mount point
+used in this container).
 """
 from __future__ import annotations
 
@@ -25,12 +32,13 @@ import tempfile
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(os.path.dirname(HERE))
-REF_TREE = "/root/reference"
+REF_TREE = os.environ.get("CUBFF_REFERENCE", "/root/reference")
 sys.path.insert(0, os.path.join(REPO, "oracle", "_ref"))
 sys.path.insert(0, REPO)
 
 import cubff  # noqa: E402  (the reference module)
 from oracle.oracle import LANGS, grid_pattern  # noqa: E402
+from cubff_gb300 import workloads  # noqa: E402
 
 
 def sha16(b) -> str:
@@ -197,8 +205,54 @@ def main(argv):
             json.dump({"generator": "tests/golden/make_golden.py long",
                        "source": "reference CPU build (oracle/_ref/cubff)", "runs": out},
                       f, indent=0)
+    elif mode in ("c2", "c3", "c4", "c5"):
+        # Full-size configurations: hash and op delta every 256 epochs (the
+        # callback fires after 0-based epochs 0, 256, 512, ...; a run stops at
+        # the first callback at or past its epoch count).
+        path = os.path.join(HERE, f"ref_{mode}.json")
+        out = json.load(open(path))["runs"] if os.path.exists(path) else {}
+        for spec in config_specs(mode):
+            if spec["name"] in out:
+                continue
+            r = ref_run(spec)
+            out[r["name"]] = r
+            print(spec["name"], r["epoch"][-1], r["sha"][-1], flush=True)
+            with open(path, "w") as f:  # after every run, so a long job can resume
+                json.dump({"generator": f"tests/golden/make_golden.py {mode}",
+                           "source": "reference CPU build (oracle/_ref/cubff)", "runs": out},
+                          f, indent=0)
     else:
-        raise SystemExit("usage: make_golden.py [small|long]")
+        raise SystemExit("usage: make_golden.py [small|long|c2|c3|c4|c5]")
+
+
+def config_specs(mode: str):
+    """The reference runs behind the full-size parity tests."""
+    if mode == "c2":
+        return [{"name": f"c2_{lang}", "lang": lang, "num_programs": 1 << 17, "seed": 1,
+                 "epochs": 16384, "callback_interval": 256} for lang in ("bff_noheads", "bff")]
+    if mode == "c3":
+        specs = [{"name": f"c3_{lang}", "lang": lang, "num_programs": 1 << 17, "seed": 2,
+                  "epochs": 4096, "callback_interval": 256}
+                 for lang in ("subleq", "rsubleq4", "forth")]
+        specs.append({"name": "c3_grid_bff_noheads", "lang": "bff_noheads",
+                      "num_programs": 512 * 256, "seed": 2, "epochs": 4096,
+                      "callback_interval": 256,
+                      "pattern": {"grid": [512, 256], "radius": 2}})
+        return specs
+    if mode == "c4":
+        return [{"name": f"c4_{s.seed}", "lang": s.lang, "num_programs": s.num_programs,
+                 "seed": s.seed, "mutation_prob": s.mutation_prob, "epochs": s.epochs,
+                 "callback_interval": 256} for s in workloads.batch_mix(2048)]
+    if mode == "c5":
+        # Every job's result is compared on the GPU alone and in the mix; this
+        # seeded sample of the 2000 jobs is also checked against the reference.
+        _, jobs = workloads.serving_jobs()
+        return [{"name": f"c5_{j}", "lang": jobs[j].lang,
+                 "num_programs": jobs[j].num_programs, "seed": jobs[j].seed,
+                 "mutation_prob": jobs[j].mutation_prob, "epochs": jobs[j].epochs,
+                 "callback_interval": jobs[j].epochs - 1}
+                for j in workloads.serving_sample()]
+    raise ValueError(mode)
 
 
 if __name__ == "__main__":

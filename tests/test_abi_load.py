@@ -44,3 +44,23 @@ def test_library_loads_and_names_languages(built_lib):
     assert L.cubff_language_name(13) is None
     assert L.cubff_status_string(abi.CUBFF_EINVAL) == b"invalid argument"
 
+
+
+def test_huge_pairing_requests_are_rejected_before_any_launch(built_lib):
+    """Sizes whose products would wrap 64 bits are refused on the host (no
+    CUDA call is made, so this runs without a GPU)."""
+    from cubff_gb300 import abi
+    L = abi.lib()
+    size_max = (1 << 64) - 1
+    assert L.cubff_shuffle_scratch_bytes(1 << 62, 1 << 31) == size_max
+    assert L.cubff_shuffle_scratch_bytes(0xffffffff, 0xffffffff) == size_max
+    assert L.cubff_shuffle_scratch_bytes(1 << 17, 64) == 24 * (1 << 17) * 64
+    fake = 1 << 20  # never dereferenced: the calls fail their argument checks
+    # 2^63 x 2 wraps to 0 when multiplied.
+    assert L.cubff_shuffle_indices_noalloc(1, 0, 2, 1 << 63, fake, None) == abi.CUBFF_EINVAL
+    assert L.cubff_shuffle_indices_noalloc(1, 0, 1 << 31, 1 << 34, fake, None) == abi.CUBFF_EINVAL
+    assert L.cubff_shuffle_indices_noalloc(1, 0, 2, (1 << 18) + 2, fake, None) == abi.CUBFF_EINVAL
+    assert L.cubff_shuffle_indices(1, 0, 0xffffffff, 0xffffffff, fake, fake, size_max,
+                                   None) == abi.CUBFF_EINVAL
+    assert L.cubff_shuffle_indices(1, 0, 2, 1 << 40, fake, fake, size_max,
+                                   None) == abi.CUBFF_EINVAL

@@ -80,7 +80,7 @@ def test_batch_matches_soups_run_alone():
 
 
 def test_batch_over_one_launch_group():
-    """More soups of one language than one launch holds (128): the run splits
+    """More soups of one language than one launch holds (64): the run splits
     them into groups on separate streams."""
     eng = abi.Engine(0)
     mix = [("bff", 2 + 2 * (k % 7), 1000 + k, 1 << 20, abi.PAIR_SHUFFLE, 0, None)

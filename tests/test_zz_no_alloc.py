@@ -61,6 +61,24 @@ def test_noalloc_back_to_back_different_sizes():
     assert torch.equal(b, _allocating(12, 3, 1, 4096))
 
 
+def test_noalloc_back_to_back_on_one_stream():
+    """Two calls queued on one non-default stream, with only that stream
+    synchronised: the second call's clearing of the shared counts is ordered
+    after the first call's kernels by the stream alone."""
+    L = abi.lib()
+    want_a = _allocating(21, 2, 8, 20000)
+    want_b = _allocating(22, 0, 2, 65536)
+    s = torch.cuda.Stream()
+    with torch.cuda.stream(s):
+        a = torch.full((8 * 20000,), -1, dtype=torch.int32, device="cuda")
+        b = torch.full((2 * 65536,), -1, dtype=torch.int32, device="cuda")
+    abi.check(L.cubff_shuffle_indices_noalloc(21, 2, 8, 20000, a.data_ptr(), s.cuda_stream))
+    abi.check(L.cubff_shuffle_indices_noalloc(22, 0, 2, 65536, b.data_ptr(), s.cuda_stream))
+    s.synchronize()
+    assert torch.equal(a.cpu(), want_a)
+    assert torch.equal(b.cpu(), want_b)
+
+
 def test_noalloc_rejects_requests_beyond_its_scratch():
     L = abi.lib()
     out = torch.empty(4 * (1 << 17), dtype=torch.int32, device="cuda")
