@@ -99,7 +99,9 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batch", action="store_true")
     ap.add_argument("--no-serving", action="store_true")
-    ap.add_argument("--serving-jobs", type=int, default=200)
+    ap.add_argument("--no-post-emergence", action="store_true")
+    ap.add_argument("--batch-epochs", type=int, default=2048)
+    ap.add_argument("--serving-jobs", type=int, default=2000)
     args = ap.parse_args()
     epochs = set_workload(args.workload)
     if args.steps is None:
@@ -170,41 +172,46 @@ class ClockSampler:
 # ---------------------------------------------------------------------------
 # Our arm.
 
-def gpu_value(torch, abi, steps: int, warmup: int, sm_mhz_hint: float, seed: int = SEED,
-              group=None):
-    """Device time of the epochs through the kernel-level C ABI on a torch
-    stream: per segment of 64 epochs, cubff_shuffle_indices (pairing) and
-    cubff_run_epochs (the pipelined epochs), bracketed by CUDA events on that
-    stream; L2 is flushed between segments, outside the events."""
+def gpu_value(torch, abi, steps: int, warmup: int, sm_mhz_hint: float = 0.0, seed: int = SEED,
+              group=None, lang: str = None, n: int = None, first: int = 0, init=None):
+    """Device time of epochs first .. first+steps-1 through the kernel-level
+    C ABI on a torch stream: per segment of 64 epochs, cubff_shuffle_indices
+    (pairing) and cubff_run_epochs (the pipelined epochs), bracketed by CUDA
+    events on that stream; L2 is flushed between segments, outside the events.
+    The soup starts as the reference's init (or `init`, host bytes of the
+    soup before epoch `first`); the warm-up runs the first `warmup` of the
+    same epochs on a scratch copy."""
     from cubff_gb300.workloads import seed_of
+    lang = LANG if lang is None else lang
+    n = N if n is None else n
     L = abi.lib()
-    lang = abi.language_id(LANG)
+    lid = abi.language_id(lang)
     dev = torch.device("cuda", 0)
     stream = torch.cuda.Stream(dev)
     sp = stream.cuda_stream
     B = 64
-    scratch = torch.empty(L.cubff_shuffle_scratch_bytes(N, B), dtype=torch.uint8, device=dev)
-    perm = torch.empty(B * N, dtype=torch.int32, device=dev)
-    ws = torch.empty(L.cubff_run_epochs_workspace_bytes(N, B), dtype=torch.uint8, device=dev)
+    scratch = torch.empty(L.cubff_shuffle_scratch_bytes(n, B), dtype=torch.uint8, device=dev)
+    perm = torch.empty(B * n, dtype=torch.int32, device=dev)
+    ws = torch.empty(L.cubff_run_epochs_workspace_bytes(n, B), dtype=torch.uint8, device=dev)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
     launches = {"n": 0}
 
-    def run(soup, first, count, counters, timed):
+    def run(soup, e0, count, counters, timed):
         ev = []
         done = 0
         while done < count:
             seg = min(B, count - done)
-            e = first + done
+            e = e0 + done
             if timed:
                 flush.fill_(done & 0xFF)  # evict the previous segment from L2
-                ev.append([torch.cuda.Event(enable_timing=True) for _ in range(3)])
+                ev.append([torch.cuda.Event(enable_timing=True) for _ in range(3)] + [seg])
                 ev[-1][0].record(stream)
-            abi.check(L.cubff_shuffle_indices(seed, e, seg, N, perm.data_ptr(), scratch.data_ptr(),
+            abi.check(L.cubff_shuffle_indices(seed, e, seg, n, perm.data_ptr(), scratch.data_ptr(),
                                               scratch.numel(), sp))
             if timed:
                 ev[-1][1].record(stream)
-            abi.check(L.cubff_run_epochs(lang, soup.data_ptr(), perm.data_ptr(), None, seed, e, seg,
-                                         MUT, N, counters.data_ptr() + 16 * done, ws.data_ptr(),
+            abi.check(L.cubff_run_epochs(lid, soup.data_ptr(), perm.data_ptr(), None, seed, e, seg,
+                                         MUT, n, counters.data_ptr() + 16 * done, ws.data_ptr(),
                                          ws.numel(), sp))
             if timed:
                 ev[-1][2].record(stream)
@@ -212,28 +219,36 @@ def gpu_value(torch, abi, steps: int, warmup: int, sm_mhz_hint: float, seed: int
             done += seg
         return ev
 
+    def fresh():
+        soup = torch.empty(n * 64, dtype=torch.uint8, device=dev)
+        if init is None:
+            abi.check(L.cubff_init_programs(seed_of(seed, 0), n, soup.data_ptr(), 0, n, sp))
+        else:
+            soup.copy_(torch.from_numpy(init).to(dev, non_blocking=False))
+        return soup
+
     with torch.cuda.stream(stream):
-        wsoup = torch.empty(N * 64, dtype=torch.uint8, device=dev)
-        abi.check(L.cubff_init_programs(seed_of(seed, 0), N, wsoup.data_ptr(), 0, N, sp))
+        wsoup = fresh()
         wcnt = torch.zeros(max(warmup, 1) * 2, dtype=torch.int64, device=dev)
-        run(wsoup, 0, warmup, wcnt, False)
+        run(wsoup, first, warmup, wcnt, False)
         stream.synchronize()
-        soup = torch.empty(N * 64, dtype=torch.uint8, device=dev)
-        abi.check(L.cubff_init_programs(seed_of(seed, 0), N, soup.data_ptr(), 0, N, sp))
+        abi.check(L.cubff_run_epochs_status(ws.data_ptr(), n, B, sp))
+        soup = fresh()
         counters = torch.zeros(steps * 2, dtype=torch.int64, device=dev)
         stream.synchronize()
         replicas.barrier(group)
         launches["n"] = 0
-        ev = run(soup, 0, steps, counters, True)
+        ev = run(soup, first, steps, counters, True)
         stream.synchronize()
         replicas.barrier(group)
-        abi.check(L.cubff_run_epochs_status(ws.data_ptr(), N, B, sp))
-    seg_ms = [x.elapsed_time(z) for x, y, z in ev]
-    kern_ms = [y.elapsed_time(z) for x, y, z in ev]
+        abi.check(L.cubff_run_epochs_status(ws.data_ptr(), n, B, sp))
+    seg_ms = [x.elapsed_time(z) for x, y, z, _ in ev]
+    kern_ms = [y.elapsed_time(z) for x, y, z, _ in ev]
     cnt = counters.view(steps, 2).cpu().numpy()
     ops, raw = cnt[:, 0].astype("uint64"), cnt[:, 1].astype("uint64")
     return {"total_s": sum(seg_ms) / 1e3, "seg_ms": seg_ms, "kern_ms": kern_ms, "ops": ops,
-            "raw": raw, "soup": soup.cpu().numpy(), "launches": launches["n"], "segments": len(ev)}
+            "raw": raw, "soup": soup.cpu().numpy(), "launches": launches["n"], "segments": len(ev),
+            "seg_epochs": [q for *_, q in ev]}
 
 
 _GRID_CACHE = {}
@@ -319,50 +334,87 @@ def gpu_e2e(torch, abi, steps: int, seed: int = SEED, group=None):
     return {"total_s": dt, "ops": ops, "raw": raw, "soup": out.numpy().copy()}
 
 
-def batch_compare(torch, abi, epochs: int):
+def _sha16(b) -> str:
+    import hashlib
+    return hashlib.sha256(bytes(b)).hexdigest()[:16]
+
+
+def _golden(name: str):
+    """Committed reference fixtures (tests/golden/<name>), or {} when absent."""
+    path = os.path.join(REPO, "tests", "golden", name)
+    if not os.path.exists(path):
+        return {}
+    with open(path) as f:
+        return json.load(f)["runs"]
+
+
+def batch_compare(torch, abi, epochs: int, peak: float):
     """The 64-soup mix (seeds 100..163): all soups in shared pipelined
     launches, one launch group per language on its own stream
     (cubff_batch_run), against one soup at a time (cubff_soup_run), same GPU,
-    same epochs; op counts and soup bytes must agree."""
+    same epochs; op counts and soup bytes must agree, and with the reference
+    fixtures present every soup's final hash is compared with its reference
+    run.  Roofline: raw interpreter steps x K_lang of every soup over the
+    batched wall time, against the measured integer-issue peak."""
     import numpy as np
     from cubff_gb300.workloads import batch_mix
     specs = batch_mix(epochs)
     eng = abi.Engine(0)
 
     def make():
-        return [abi.Soup(eng, s.lang, s.num_programs, s.seed, s.mutation_prob) for s in specs]
+        soups = []
+        for s in specs:
+            soup = abi.Soup(eng, s.lang, s.num_programs, s.seed, s.mutation_prob)
+            init = soup.read()
+            soup.run(1)  # pairing buffers allocated outside the timed region
+            soup.set_epoch(0, 1)
+            soup.write(init.tobytes())
+            soups.append(soup)
+        return soups
 
     soups = make()
-    for s in soups:  # pairing buffers allocated outside the timed region
-        s.run(1)
-        s.set_epoch(0, 1)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    seq_ops = [s.run(epochs)[0] for s in soups]
+    seq = [s.run(epochs) for s in soups]
     torch.cuda.synchronize()
     t_seq = time.perf_counter() - t0
-    seq_sha = [hash(s.read().tobytes()) for s in soups]
+    seq_sha = [_sha16(s.read()) for s in soups]
     for s in soups:
         s.close()
     soups = make()
-    for s in soups:
-        s.run(1)
-        s.set_epoch(0, 1)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     bops = abi.batch_run(eng, soups, epochs)
     torch.cuda.synchronize()
     t_bat = time.perf_counter() - t0
-    bat_sha = [hash(s.read().tobytes()) for s in soups]
+    bat_sha = [_sha16(s.read()) for s in soups]
     for s in soups:
         s.close()
     eng.close()
-    same = all(np.array_equal(a, b) for a, b in zip(seq_ops, bops)) and seq_sha == bat_sha
-    total_ops = float(sum(int(x.sum()) for x in seq_ops))
+    same = all(np.array_equal(a[0], b) for a, b in zip(seq, bops)) and seq_sha == bat_sha
+    total_ops = float(sum(int(x[0].sum()) for x in seq))
+    work = float(sum(int(x[1].sum()) * K_LANG[sp.lang] for x, sp in zip(seq, specs)))
+    ref = _golden("ref_c4.json")
+    vs_ref = None
+    if ref and all(f"c4_{sp.seed}" in ref for sp in specs):
+        vs_ref = True
+        for sp, sha, ops in zip(specs, bat_sha, bops):
+            r = ref[f"c4_{sp.seed}"]
+            if r["epoch"][-1] == epochs:
+                vs_ref &= sha == r["sha"][-1] and int(ops.sum()) == sum(r["ops"])
+            else:
+                vs_ref = None
+                break
     return {"soups": len(specs), "epochs": epochs,
             "programs_total": int(sum(s.num_programs for s in specs)),
             "per_soup_steps_per_s": total_ops / t_seq, "batched_steps_per_s": total_ops / t_bat,
-            "batched_over_per_soup": t_seq / t_bat, "bit_identical": bool(same)}
+            "per_soup_s": t_seq, "batched_s": t_bat,
+            "batched_over_per_soup": t_seq / t_bat, "bit_identical": bool(same),
+            "bit_identical_vs_reference": vs_ref,
+            "roofline": {"bound": "int_issue", "achieved": work / t_bat / 1e12,
+                         "peak": peak / 1e12, "unit": "T int-instr/s",
+                         "frac": work / t_bat / peak,
+                         "work": "raw interpreter steps x K_lang of every soup, batched wall time"}}
 
 
 def serving_sample(torch, abi, jobs: int, verify: int = 4):
@@ -397,23 +449,27 @@ def serving_sample(torch, abi, jobs: int, verify: int = 4):
     return out
 
 
-def cpu_sample(budget_s: float = 15.0, max_epochs: int = 10**9):
+def cpu_sample(budget_s: float = 20.0, max_epochs: int = 10**9, nthreads: int = 0):
     """The reference's CPU implementation (its own build when it was compiled
-    on this machine, else the oracle port) on this host's cores, epochs 0..E of
-    the benchmark workload, stopped after ~budget_s."""
+    on this machine, else the oracle port) on this host's cores: epochs
+    0 .. max_epochs-1 of the benchmark workload, the same epochs the GPU arm
+    times, cut short after ~budget_s.  nthreads = 1 times one core (the port
+    only)."""
     kind = "port"
     ref_dir = os.path.join(REPO, "oracle", "_ref")
-    cores = os.cpu_count() or 1
+    cores = nthreads or os.cpu_count() or 1
     ops_total, epochs_run, t_used = 0, 0, 0.0
-    try:
-        sys.path.insert(0, ref_dir)
-        import cubff as refmod  # the reference module, where it was built here
-        kind = "reference"
-    except ImportError:
-        refmod = None
-    finally:
-        if ref_dir in sys.path:
-            sys.path.remove(ref_dir)
+    refmod = None
+    if nthreads == 0:
+        try:
+            sys.path.insert(0, ref_dir)
+            import cubff as refmod  # the reference module, where it was built here
+            kind = "reference"
+        except ImportError:
+            refmod = None
+        finally:
+            if ref_dir in sys.path:
+                sys.path.remove(ref_dir)
     if refmod is not None and PATTERN is None:
         p = refmod.SimulationParams()
         p.num_programs, p.seed, p.mutation_prob, p.callback_interval = N, SEED, MUT, 1
@@ -437,33 +493,91 @@ def cpu_sample(budget_s: float = 15.0, max_epochs: int = 10**9):
             st["ep"] = e
             return (time.perf_counter() - t0 > budget_s) or e >= max_epochs
         if PATTERN is None:
-            O.OracleSim(LANG, N, SEED, MUT).run(cb)
+            O.OracleSim(LANG, N, SEED, MUT, nthreads=nthreads).run(cb)
         else:
             from cubff_gb300.workloads import grid_pattern
             O.OracleSim(LANG, N, SEED, MUT, pairing=O.PAIR_PATTERN,
-                        pattern=grid_pattern(*PATTERN)).run(cb)
+                        pattern=grid_pattern(*PATTERN), nthreads=nthreads).run(cb)
         t_used = time.perf_counter() - t0
         ops_total, epochs_run = st["ops"], st["ep"]
     return {"value": ops_total / t_used, "unit": "steps/s", "cores": cores, "kind": kind,
+            "epochs": epochs_run,
             "sample": f"{LANG} {_log2(N)} programs seed {SEED}, epochs 0..{epochs_run - 1} "
                       f"({t_used:.1f} s, callback per epoch)"}
 
 
+def post_emergence(torch, abi, peak: float, start: int = 5121, epochs: int = 256,
+                   warmup: int = 8):
+    """bff (two heads), 2^17 programs, seed 1 after self-replicators emerged:
+    the soup is run to epoch `start` through the soup API and its hash checked
+    against the reference's; then epochs start .. start+epochs-1 are timed as
+    the headline is (kernel-level C ABI, CUDA events), and the hash after them
+    is checked against the reference's again."""
+    ref = _golden("ref_long.json").get("long_bff")
+    if not ref or start not in ref["epoch"] or start + epochs not in ref["epoch"]:
+        return {"unavailable": "reference hashes of bff 2^17 seed 1 not committed"}
+    eng = abi.Engine(0)
+    soup = abi.Soup(eng, "bff", 1 << 17, 1, MUT)
+    soup.run(start)
+    init = soup.read()
+    soup.close()
+    eng.close()
+    start_ok = _sha16(init) == ref["sha"][ref["epoch"].index(start)]
+    gv = gpu_value(torch, abi, epochs, warmup, lang="bff", n=1 << 17, seed=1, first=start,
+                   init=init)
+    end_ok = _sha16(gv["soup"]) == ref["sha"][ref["epoch"].index(start + epochs)]
+    ops_ok = int(gv["ops"].sum()) == ref["ops"][ref["epoch"].index(start + epochs)]
+    kern_s = float(sum(gv["kern_ms"])) / 1e3
+    raw = float(gv["raw"].astype(float).sum())
+    return {"workload": f"bff 2^17 programs, seed 1, mutation 2^-12, epochs {start}.."
+                        f"{start + epochs - 1} (after self-replicator emergence)",
+            "value": float(gv["ops"].sum()) / gv["total_s"], "unit": "steps/s",
+            "raw_steps_per_s": raw / gv["total_s"],
+            "ms_per_epoch": gv["total_s"] * 1e3 / epochs,
+            "roofline": {"bound": "int_issue", "achieved": raw * K_LANG["bff"] / kern_s / 1e12,
+                         "peak": peak / 1e12, "unit": "T int-instr/s",
+                         "frac": raw * K_LANG["bff"] / kern_s / peak},
+            "start_hash_matches_reference": start_ok,
+            "end_hash_and_ops_match_reference": bool(end_ok and ops_ok)}
+
+
 DRAW_OPS = 21  # 32-bit integer ops of one SplitMix64 mutation draw + its threshold test
-# DRAM traffic of one 64-epoch pipelined launch of this workload (2^17 programs), from an ncu
-# capture: dram__bytes_read.sum + dram__bytes_write.sum = 175.4 MB + 24.7 MB.
-NCU_DRAM_BYTES_PER_LAUNCH = 199.1e6
 
 
-def roofline(gv, peaks, peaks_src, sm_mhz):
-    """Integer-issue roofline of the pipelined epoch launch.  achieved = the
-    integer work the reference algorithm does for these epochs (every raw
-    interpreter iteration x K_lang, plus 128 SplitMix64 mutation draws per
-    pair x DRAW_OPS) per second of launch time; peak = SMs x 128 lane-int-ops
-    per clock x the maximum SM clock.  Runs of no-ops crossed in one step and
-    fast-forwarded cycles are counted at their reference cost, so this is the
-    rate at which the reference's work gets done."""
-    import numpy as np
+def int_issue_peak(abi):
+    """Measured integer-issue peak (lane-instructions/s) of this GPU: the
+    larger of the two chains cubff_measure_int_issue times."""
+    alu, mixed = abi.measure_int_issue(0)
+    return max(alu, mixed), {"alu_tops": alu / 1e12, "mixed_tops": mixed / 1e12}
+
+
+def profiled_traffic(seg_epochs):
+    """DRAM bytes per pipelined launch from the committed ncu summaries under
+    profiles/ (a line `traffic: workload=<lang>-<n> epochs_per_launch=<E>
+    dram_bytes_per_launch=<B>`), when one matches every timed launch."""
+    import glob
+    import re
+    if not seg_epochs or len(set(seg_epochs)) != 1:
+        return None, None
+    want = (f"{LANG}-{N}", int(seg_epochs[0]))
+    for path in sorted(glob.glob(os.path.join(REPO, "profiles", "*.txt"))):
+        with open(path) as f:
+            for line in f:
+                m = re.match(r"traffic: workload=(\S+) epochs_per_launch=(\d+) "
+                             r"dram_bytes_per_launch=(\d+)", line.strip())
+                if m and (m.group(1), int(m.group(2))) == want:
+                    return float(m.group(3)), os.path.relpath(path, REPO)
+    return None, None
+
+
+def roofline(gv, peaks, peaks_src, peak, peak_detail):
+    """Integer-issue roofline of the pipelined epoch launches.  achieved =
+    raw interpreter steps x K_lang per second of launch time (the unit of
+    work the reference's interpreter loop does: runs of no-ops crossed in one
+    step and fast-forwarded cycles count at their reference cost); peak = the
+    integer-instruction rate measured on this GPU (int_issue_peak).  Also
+    given: the same against the nominal 128 lanes/clk/SM, and a variant that
+    also credits the 128 SplitMix64 mutation draws per pair."""
     sms = 152
     try:
         import torch
@@ -471,27 +585,33 @@ def roofline(gv, peaks, peaks_src, sm_mhz):
     except Exception:
         pass
     clk = float(peaks.get("sm_max_mhz", 2070.0))
-    peak = sms * 128 * clk * 1e6 / 1e12           # T int-op/s
-    kern_s = float(np.sum(gv["kern_ms"])) / 1e3
+    nominal = sms * 128 * clk * 1e6
+    kern_s = float(sum(gv["kern_ms"])) / 1e3
     epochs = len(gv["ops"])
-    work = float(gv["raw"].astype(float).sum()) * K_LANG[LANG] + (N // 2) * 128.0 * DRAW_OPS * epochs
-    achieved = work / kern_s / 1e12
-    return {"bound": "int_issue", "achieved": achieved, "peak": peak, "unit": "Tintop/s",
-            "frac": achieved / peak,
-            "traffic": NCU_DRAM_BYTES_PER_LAUNCH if (LANG, N) == ("bff_noheads", 1 << 17) else None,
-            "traffic_unit": "bytes per 64-epoch launch (ncu capture)",
-            "algorithmic_bytes_per_launch": 264.0 * (N // 2) * 64,
-            "peak_source": f"{sms} SMs x 128 x {clk:.0f} MHz ({peaks_src} sm_max_mhz)",
-            "work_per_launch_Tintop": work / len(gv["kern_ms"]) / 1e12,
+    work = float(gv["raw"].astype(float).sum()) * K_LANG[LANG]
+    draws = (N // 2) * 128.0 * DRAW_OPS * epochs
+    traffic, traffic_src = profiled_traffic(gv.get("seg_epochs"))
+    hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
+    hbm = 264.0 * (N // 2) * epochs / kern_s / 1e9
+    return {"bound": "int_issue", "achieved": work / kern_s / 1e12, "peak": peak / 1e12,
+            "unit": "T int-instr/s", "frac": work / kern_s / peak,
+            "traffic": traffic,
+            "traffic_unit": "DRAM bytes per pipelined launch (ncu dram__bytes_read.sum + "
+                            "dram__bytes_write.sum)",
+            "traffic_source": traffic_src,
+            "algorithmic_bytes_per_launch": 264.0 * (N // 2) * epochs / len(gv["kern_ms"]),
+            "peak_source": "measured on this GPU by cubff_measure_int_issue (max of an add/xor "
+                           "chain and an add/xor/multiply-add chain)",
+            "peak_chains": peak_detail,
+            "peak_nominal": nominal / 1e12,
+            "frac_of_nominal": work / kern_s / nominal,
+            "nominal_source": f"{sms} SMs x 128 lanes/clk x {clk:.0f} MHz ({peaks_src})",
+            "achieved_with_draws": (work + draws) / kern_s / 1e12,
+            "frac_with_draws": (work + draws) / kern_s / peak,
             "launch_mean_ms": kern_s * 1e3 / len(gv["kern_ms"]),
             "epochs_per_launch": epochs / len(gv["kern_ms"]),
-            "hbm_gbs_secondary": 264.0 * (N // 2) * epochs / kern_s / 1e9,
-            # The same launches against the measured HBM copy bandwidth
-            # (algorithmic bytes: 264 B per pair-epoch): the memory side is
-            # far from binding.
-            "hbm": {"bound": "hbm", "achieved": 264.0 * (N // 2) * epochs / kern_s / 1e9,
-                    "peak": float(peaks.get("hbm_gbs", 6800.0)), "unit": "GB/s",
-                    "frac": 264.0 * (N // 2) * epochs / kern_s / 1e9 / float(peaks.get("hbm_gbs", 6800.0)),
+            "hbm": {"bound": "hbm", "achieved": hbm, "peak": hbm_peak, "unit": "GB/s",
+                    "frac": hbm / hbm_peak,
                     "peak_source": f"MEASURED_PEAKS.json hbm_gbs ({peaks_src})"}}
 
 
@@ -520,10 +640,10 @@ def main():
     seed = replicas.replica_seed(SEED, rank)  # independent replicas: one soup per GPU
     abi.lib()
     peaks, src = measured_peaks()
+    peak, peak_detail = int_issue_peak(abi)
     with ClockSampler(local) as clocks:
         if PATTERN is None:
-            gv = gpu_value(torch, abi, args.steps, args.warmup, peaks.get("sm_max_mhz", 2070.0),
-                           seed, group)
+            gv = gpu_value(torch, abi, args.steps, args.warmup, seed=seed, group=group)
         else:
             gv = gpu_soup_value(torch, abi, args.steps, args.warmup, seed, group)
     ck = clocks.summary()
@@ -542,7 +662,7 @@ def main():
             "raw_steps_per_s": raw_all / t_dev,
             "pairs_per_s": (N // 2) * args.steps * world / t_dev,
             "gpu_launches": gv["launches"],
-            "roofline": roofline(gv, peaks, src, ck.get("sm_mhz")),
+            "roofline": roofline(gv, peaks, src, peak, peak_detail),
             "clocks": ck,
             "e2e": {"value": ops_e2e / t_e2e, "unit": "steps/s",
                     "h2d_bytes_per_step": N * 64 / args.steps,
@@ -550,12 +670,21 @@ def main():
                     "wall_s": t_e2e}}
     if world > 1:
         line["replicas"] = f"{world} independent soups (seeds {SEED}..{SEED + world - 1}), one per GPU"
+    log = lambda msg: print(f"[bench] {msg}", file=sys.stderr, flush=True)  # noqa: E731
+    log(f"headline {line['value']:.4g} steps/s, frac {line['roofline']['frac']:.4f}")
+    if rank == 0 and not args.no_post_emergence and PATTERN is None:
+        line["post_emergence"] = post_emergence(torch, abi, peak)
+        log(f"post-emergence {line['post_emergence']}")
     if rank == 0 and not args.no_batch:
-        line["batched"] = batch_compare(torch, abi, 64)
+        line["batched"] = batch_compare(torch, abi, args.batch_epochs, peak)
+        log(f"batched {line['batched']}")
     if rank == 0 and not args.no_serving:
         line["serving"] = serving_sample(torch, abi, args.serving_jobs)
+        log(f"serving {line['serving']}")
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_sample()
+        line["cpu_baseline"] = cpu_sample(max_epochs=args.steps)
+        one = cpu_sample(budget_s=10.0, max_epochs=args.steps, nthreads=1)
+        line["cpu_baseline"]["one_core"] = {k: one[k] for k in ("value", "cores", "kind", "sample")}
     if rank == 0:
         print(json.dumps(line))
     if group is not None:

@@ -8,6 +8,7 @@ from __future__ import annotations
 
 import ctypes
 import os
+import weakref
 from typing import Optional
 
 import numpy as np
@@ -26,6 +27,15 @@ u64, u32, vp, ci, cp, sz = (ctypes.c_uint64, ctypes.c_uint32, ctypes.c_void_p, c
 class SoupParams(ctypes.Structure):
     _fields_ = [("lang", ci), ("num_programs", u64), ("seed", u64), ("mutation_prob", u32),
                 ("pairing", ci), ("reset_interval", u64), ("zero_init", ci)]
+
+
+class Tuning(ctypes.Structure):
+    """cubff_tuning: the launch shape of a pipelined launch."""
+    _fields_ = [("lanes_per_pair64", u32), ("steps_per_visit", u32), ("claim_min", u32),
+                ("long_visits", u32)]
+
+    def as_dict(self):
+        return {f: int(getattr(self, f)) for f, _ in self._fields_}
 
 
 class JobInfo(ctypes.Structure):
@@ -51,6 +61,14 @@ SIGNATURES = {
     "cubff_run_epochs": (ci, [ci, vp, vp, vp, u64, u64, u32, u32, u64, vp, vp, sz, vp]),
     "cubff_run_epochs_status": (ci, [vp, u64, u32, vp]),
     "cubff_set_wait_limit_ns": (ci, [u64, ctypes.POINTER(u64)]),
+    "cubff_default_tuning": (None, [ctypes.POINTER(Tuning)]),
+    "cubff_run_epochs_tuned": (ci, [ci, vp, vp, vp, u64, u64, u32, u32, u64, vp, vp, sz,
+                                    ctypes.POINTER(Tuning), vp]),
+    "cubff_engine_tune": (ci, [vp, vp, ci, u32, ctypes.POINTER(Tuning)]),
+    "cubff_engine_get_tuning": (ci, [vp, ci, u64, u32, ctypes.POINTER(Tuning)]),
+    "cubff_engine_set_tuning": (ci, [vp, ci, u64, u32, ctypes.POINTER(Tuning)]),
+    "cubff_measure_int_issue": (ci, [ci, ctypes.POINTER(ctypes.c_double),
+                                     ctypes.POINTER(ctypes.c_double)]),
     "cubff_engine_create": (ci, [ci, ctypes.POINTER(vp)]),
     "cubff_engine_destroy": (ci, [vp]),
     "cubff_soup_create": (ci, [vp, ctypes.POINTER(SoupParams), ctypes.POINTER(vp)]),
@@ -121,9 +139,31 @@ class Engine:
         h = vp()
         check(lib().cubff_engine_create(device, ctypes.byref(h)))
         self.h = h
+        self._soups = weakref.WeakSet()  # destroyed before the engine
+
+    def tune(self, soups, trial_epochs: int = 16):
+        """Tunes the launch shape of the launch groups these soups form
+        (cubff_engine_tune); returns each soup's shape as a dict."""
+        arr = (vp * len(soups))(*[s.h for s in soups])
+        out = (Tuning * len(soups))()
+        check(lib().cubff_engine_tune(self.h, arr, len(soups), trial_epochs, out))
+        return [out[i].as_dict() for i in range(len(soups))]
+
+    def get_tuning(self, lang: str, group_programs: int, group_soups: int = 1) -> dict:
+        t = Tuning()
+        check(lib().cubff_engine_get_tuning(self.h, language_id(lang), group_programs,
+                                            group_soups, ctypes.byref(t)))
+        return t.as_dict()
+
+    def set_tuning(self, lang: str, group_programs: int, group_soups: int, **knobs):
+        t = Tuning(**{**self.get_tuning(lang, group_programs, group_soups), **knobs})
+        check(lib().cubff_engine_set_tuning(self.h, language_id(lang), group_programs,
+                                            group_soups, ctypes.byref(t)))
 
     def close(self):
         if self.h:
+            for s in list(self._soups):
+                s.close()
             lib().cubff_engine_destroy(self.h)
             self.h = None
 
@@ -147,6 +187,7 @@ class Soup:
         h = vp()
         check(lib().cubff_soup_create(engine.h, ctypes.byref(self.params), ctypes.byref(h)))
         self.h = h
+        engine._soups.add(self)
 
     def set_pattern(self, offs: np.ndarray, tgts: np.ndarray):
         offs = np.ascontiguousarray(offs, dtype=np.uint32)
@@ -197,12 +238,26 @@ class Soup:
             pass
 
 
+def default_tuning() -> dict:
+    t = Tuning()
+    lib().cubff_default_tuning(ctypes.byref(t))
+    return t.as_dict()
+
+
 def set_wait_limit_ns(ns: int) -> int:
     """Sets the bound of the waits inside pipelined launches; returns the
     previous bound (cubff_set_wait_limit_ns)."""
     prev = u64(0)
     check(lib().cubff_set_wait_limit_ns(ns, ctypes.byref(prev)))
     return int(prev.value)
+
+
+def measure_int_issue(device: int = 0):
+    """(alu, mixed) integer lane-instructions per second measured on the
+    device (cubff_measure_int_issue)."""
+    a, m = ctypes.c_double(0), ctypes.c_double(0)
+    check(lib().cubff_measure_int_issue(device, ctypes.byref(a), ctypes.byref(m)))
+    return a.value, m.value
 
 
 def batch_run(engine: Engine, soups, n_epochs: int) -> np.ndarray:

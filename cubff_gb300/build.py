@@ -28,7 +28,8 @@ REPO = os.path.dirname(PKG)
 BUILD = os.path.join(PKG, "_build", platform.machine())
 LIB = os.path.join(PKG, "libcubff_gb300.so")
 
-CUDA_SOURCES = ["epoch.cu", "pairing.cu", "pipeline.cu", "engine.cu", "batch.cu", "server.cu"]
+CUDA_SOURCES = ["epoch.cu", "pairing.cu", "pipeline.cu", "engine.cu", "batch.cu", "server.cu",
+                "calib.cu", "tune.cu"]
 HOST_SOURCES = ["host/lang_host.cc", "host/simulation.cc"]  # C++ simulation API
 PY_SOURCES = ["host/cubff_py.cc"]                            # the `cubff` module
 CLI_SOURCES = ["host/main.cc"]                               # cubff_main

@@ -86,6 +86,7 @@ struct Group {
   std::vector<int> members;  // indices into the run's soups
   cudaStream_t st;
   size_t qoff;               // first entry of the group's ready queue in d_queue
+  uint64_t programs = 0;     // summed over the members (the launch-shape key)
 };
 
 // Per-soup progress of a run.
@@ -140,8 +141,14 @@ static int copy_counters(cubff_soup *const *soups, const std::vector<Group> &gro
 }
 
 int run_soups(cubff_engine *eng, cubff_soup *const *soups, int n_soups, uint64_t n_epochs,
-              uint64_t *const *ops, uint64_t *const *raw, uint64_t *const *ni) {
-  if (n_epochs == 0 || n_soups == 0) return CUBFF_OK;
+              uint64_t *const *ops, uint64_t *const *raw, uint64_t *const *ni,
+              const uint64_t *epochs_each) {
+  if (n_soups == 0) return CUBFF_OK;
+  // Epochs soup i advances: its own count, or n_epochs for all.
+  auto want = [&](int i) { return epochs_each ? epochs_each[i] : n_epochs; };
+  bool any_work = false;
+  for (int i = 0; i < n_soups; i++) any_work |= want(i) > 0;
+  if (!any_work) return CUBFF_OK;
   constexpr uint64_t kChunk = cubff_soup::kCounterChunk;
   for (int i = 0; i < n_soups; i++) CUBFF_TRY(soups[i]->ensure_buffers());
 
@@ -155,8 +162,9 @@ int run_soups(cubff_engine *eng, cubff_soup *const *soups, int n_soups, uint64_t
   for (int i : order) {
     if (groups.empty() || groups.back().lang != soups[i]->p.lang ||
         groups.back().members.size() == size_t(kMaxPipeSoups))
-      groups.push_back(Group{soups[i]->p.lang, {}, nullptr, entries});
+      groups.push_back(Group{soups[i]->p.lang, {}, nullptr, entries, 0});
     groups.back().members.push_back(i);
+    groups.back().programs += soups[i]->p.num_programs;
     entries += size_t(soups[i]->batch) * (soups[i]->p.num_programs / 2);
   }
   const size_t G = groups.size();
@@ -185,14 +193,15 @@ int run_soups(cubff_engine *eng, cubff_soup *const *soups, int n_soups, uint64_t
   }
 
   std::vector<Progress> pr(n_soups);
-  const uint64_t first_rows = std::min<uint64_t>(n_epochs, kChunk);
   for (const Group &g : groups) {
     for (int i : g.members) {
       cubff_soup *s = soups[i];
+      if (want(i) == 0) continue;
       if (s->pending_reset) {
         CUBFF_TRY(s->apply_reset(g.st));
         s->pending_reset = false;
       }
+      const uint64_t first_rows = std::min<uint64_t>(want(i), kChunk);
       CUBFF_CUDA_TRY(cudaMemsetAsync(s->d_counters, 0,
                                      first_rows * kPipeCountSlots * 2 * sizeof(unsigned long long),
                                      g.st));
@@ -205,7 +214,7 @@ int run_soups(cubff_engine *eng, cubff_soup *const *soups, int n_soups, uint64_t
     // A soup whose counter chunk is full: read every soup's counters back.
     bool flush = false;
     for (int i = 0; i < n_soups; i++)
-      flush |= pr[i].done < n_epochs && pr[i].done - pr[i].cbase == kChunk;
+      flush |= pr[i].done < want(i) && pr[i].done - pr[i].cbase == kChunk;
     if (flush) {
       CUBFF_TRY(copy_counters(soups, groups, pr, eng));
       for (const Group &g : groups) CUBFF_CUDA_TRY(cudaStreamSynchronize(g.st));
@@ -214,7 +223,7 @@ int run_soups(cubff_engine *eng, cubff_soup *const *soups, int n_soups, uint64_t
       for (const Group &g : groups) {
         for (int i : g.members) {
           pr[i].cbase = pr[i].done;
-          const uint64_t rows = std::min<uint64_t>(n_epochs - pr[i].done, kChunk);
+          const uint64_t rows = std::min<uint64_t>(want(i) - pr[i].done, kChunk);
           if (rows)
             CUBFF_CUDA_TRY(cudaMemsetAsync(soups[i]->d_counters, 0,
                                            rows * kPipeCountSlots * 2 * sizeof(unsigned long long),
@@ -234,13 +243,13 @@ int run_soups(cubff_engine *eng, cubff_soup *const *soups, int n_soups, uint64_t
         cubff_soup *s = soups[i];
         Progress &p = pr[i];
         p.seg = 0;
-        if (p.done >= n_epochs) continue;
+        if (p.done >= want(i)) continue;
         const uint64_t n = s->p.num_programs, P = n / 2;
         const uint64_t e = s->epoch + p.done;
         if (s->perm_count == 0 || e < s->perm_first || e >= s->perm_first + s->perm_count)
-          CUBFF_TRY(s->fill_pairing(e, static_cast<uint32_t>(std::min<uint64_t>(s->batch, n_epochs - p.done)),
+          CUBFF_TRY(s->fill_pairing(e, static_cast<uint32_t>(std::min<uint64_t>(s->batch, want(i) - p.done)),
                                     g.st));
-        uint64_t seg = std::min<uint64_t>(s->perm_first + s->perm_count - e, n_epochs - p.done);
+        uint64_t seg = std::min<uint64_t>(s->perm_first + s->perm_count - e, want(i) - p.done);
         seg = std::min<uint64_t>(seg, p.cbase + kChunk - p.done);
         if (s->p.reset_interval) {
           const uint64_t r = e + (s->p.reset_interval - e % s->p.reset_interval) % s->p.reset_interval;
@@ -289,14 +298,16 @@ int run_soups(cubff_engine *eng, cubff_soup *const *soups, int n_soups, uint64_t
       q.lang = g.lang;
       pb.error = reinterpret_cast<int *>(eng->d_ctl + 4 * gi + 2);
       pb.wait_limit_ns = pipeline_wait_limit_ns();
+      const cubff_tuning shape = eng->shape_for(g.lang, g.programs, static_cast<uint32_t>(g.members.size()));
+      pb.tune = pipe_tuning(shape);
       CUBFF_CUDA_TRY(cudaMemsetAsync(q.ctl, 0, 2 * sizeof(uint32_t), g.st));  // head, tail
-      CUBFF_TRY(launch_pipeline(pb, pairs, eng->lanes_per_pair64, eng->device, g.st));
+      CUBFF_TRY(launch_pipeline(pb, pairs, shape.lanes_per_pair64, eng->device, g.st));
       // Pattern pairings are built on the host: build the next batch of a
       // soup whose run goes on past its cached one while this launch runs.
       for (int i : g.members) {
         cubff_soup *s = soups[i];
         if (s->p.pairing != CUBFF_PAIR_PATTERN || pr[i].seg == 0) continue;
-        const uint64_t next = s->perm_first + s->perm_count, end = s->epoch + n_epochs;
+        const uint64_t next = s->perm_first + s->perm_count, end = s->epoch + want(i);
         if (next < end && !(s->pat_worker.joinable() && s->pat_pf_first == next))
           CUBFF_TRY(s->prefetch_pattern(next, static_cast<uint32_t>(std::min<uint64_t>(s->batch, end - next))));
       }
@@ -307,7 +318,7 @@ int run_soups(cubff_engine *eng, cubff_soup *const *soups, int n_soups, uint64_t
         const uint64_t last = s->epoch + p.done + p.seg - 1;
         p.done += p.seg;
         if (s->p.reset_interval && last % s->p.reset_interval == 0) {
-          if (p.done == n_epochs) s->pending_reset = true;
+          if (p.done == want(i)) s->pending_reset = true;
           else CUBFF_TRY(s->apply_reset(g.st));
         }
       }

@@ -62,13 +62,25 @@ __device__ __forceinline__ uint32_t lane_base(uint32_t tid) {
 // leave the thread's own 128 bytes: every interpreter keeps its positions in
 // 0..127 anyway, and the parity tests would show any position that relied on
 // the wrap.
+#ifdef CUBFF_HOST_INDEX_CHECK
+// Host-compiled analysis builds only: reports every position outside the
+// accessor's range before it is wrapped or clamped.
+void cubff_index_violation(int kind, int p);
+#define CUBFF_CHECK_POS(kind, p, hi) \
+  do { if ((p) < 0 || (p) > (hi)) cubff_index_violation((kind), (p)); } while (0)
+#else
+#define CUBFF_CHECK_POS(kind, p, hi) do { } while (0)
+#endif
+
 struct LaneBytes {
   uint8_t *s;     // dynamic shared memory block holding the layout
   uint32_t base;  // lane_base(tid)
   __host__ __device__ __forceinline__ uint32_t get(int p) const {
+    CUBFF_CHECK_POS(0, p, kPair - 1);
     return s[base + ((static_cast<uint32_t>(p) & (kPair - 1)) << 7)];
   }
   __host__ __device__ __forceinline__ void set(int p, uint32_t v) const {
+    CUBFF_CHECK_POS(1, p, kPair - 1);
     s[base + ((static_cast<uint32_t>(p) & (kPair - 1)) << 7)] = static_cast<uint8_t>(v);
   }
 };
@@ -92,9 +104,11 @@ struct LaneNp {
     return q < kNpEntries - 1 ? q : kNpEntries - 1;
   }
   __host__ __device__ __forceinline__ uint32_t get(int p) const {
+    CUBFF_CHECK_POS(2, p, kNpEntries - 1);
     return s[base + (clamp(p) << 7)];
   }
   __host__ __device__ __forceinline__ void set(int p, uint32_t v) const {
+    CUBFF_CHECK_POS(3, p, kNpEntries - 1);
     s[base + (clamp(p) << 7)] = static_cast<uint16_t>(v);
   }
 };

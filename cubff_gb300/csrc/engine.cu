@@ -362,7 +362,6 @@ int cubff_engine_create(int device, cubff_engine **out) {
   auto *e = new (std::nothrow) cubff_engine();
   if (!e) return set_error(CUBFF_ENOMEM, "engine_create: host allocation");
   e->device = device;
-  if (const char *v = std::getenv("CUBFF_LANES_PER_PAIR64")) e->lanes_per_pair64 = std::atoi(v);
   cudaError_t err = cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking);
   if (err != cudaSuccess) {
     delete e;

@@ -2,6 +2,7 @@
 #pragma once
 
 #include <cstdint>
+#include <map>
 #include <thread>
 #include <vector>
 
@@ -12,7 +13,13 @@
 struct cubff_engine {
   int device = 0;
   cudaStream_t stream = nullptr;
-  uint32_t lanes_per_pair64 = 0;  // pipelined-run lanes in flight per 64 pairs (0 = default)
+
+  // Launch shapes by launch-group key (shape_key), set by the tuner or by
+  // hand; `forced` (the tuner's trials) overrides them all.
+  std::map<uint64_t, cubff_tuning> shapes;
+  const cubff_tuning *forced = nullptr;
+  static uint64_t shape_key(int lang, uint64_t group_programs, uint32_t group_soups);
+  cubff_tuning shape_for(int lang, uint64_t group_programs, uint32_t group_soups) const;
 
   // Pipelined runs (batch.cu).  A run splits its soups into launch groups
   // (one language, at most kMaxPipeSoups soups); group g runs on streams[g],
@@ -88,9 +95,11 @@ struct cubff_soup {
 namespace cubff {
 using Soup = cubff_soup;
 
-// Advances every soup by n_epochs epochs in pipelined launches (batch.cu).
-// ops / raw / ni: per-soup host arrays of n_epochs entries (each nullable):
-// op count, raw interpreter iterations and evaluated pairs of each epoch.
+// Advances every soup by n_epochs epochs (soup i by epochs_each[i] when that
+// is given) in pipelined launches (batch.cu).  ops / raw / ni: per-soup host
+// arrays with an entry per epoch it advances (each nullable): op count, raw
+// interpreter iterations and evaluated pairs of each epoch.
 int run_soups(cubff_engine *eng, cubff_soup *const *soups, int n_soups, uint64_t n_epochs,
-              uint64_t *const *ops, uint64_t *const *raw, uint64_t *const *ni);
+              uint64_t *const *ops, uint64_t *const *raw, uint64_t *const *ni,
+              const uint64_t *epochs_each = nullptr);
 }

@@ -73,6 +73,23 @@ struct PipeQueue {
 // (grid-constant) parameter, so that a launch needs no host-to-device copy
 // and can be captured in a CUDA graph.  All soups have the queue's language;
 // the queue serves soups [first_soup, first_soup + n_soups) = all of them.
+// Launch-shape knobs of a pipelined launch (the tuner's search space, with
+// lanes in flight per 64 pairs; results never depend on them).
+struct PipeTuning {
+  uint32_t steps_per_visit;  // interpreter steps a running lane takes per warp iteration
+  uint32_t claim_min;        // idle lanes a busy warp needs before it claims new pairs
+  uint32_t long_visits;      // visits after which a pair counts as long: its warp stops
+                             // claiming, so the pair runs without new warp-mates
+};
+// The default launch shape (cubff_tuning: lanes in flight per 64 pairs, then
+// the PipeTuning knobs; long_visits 0 = never), each knob overridable by the
+// environment (CUBFF_LANES_PER_PAIR64, CUBFF_STEPS_PER_VISIT, CUBFF_CLAIM_MIN,
+// CUBFF_LONG_VISITS), read once.
+cubff_tuning default_shape();
+// The kernel's view of a shape; false when a knob is out of range.
+bool valid_shape(const cubff_tuning &t);
+PipeTuning pipe_tuning(const cubff_tuning &t);
+
 constexpr int kMaxPipeSoups = 64;
 struct PipeBatch {
   PipeSoup soups[kMaxPipeSoups];
@@ -80,6 +97,7 @@ struct PipeBatch {
   int n_soups;
   int *error;                   // 1: a bounded wait gave up; 2: a bad queue entry
   uint64_t wait_limit_ns;       // bound of every wait inside the launch
+  PipeTuning tune;
 };
 // The wait bound given to pipelined launches (cubff_set_wait_limit_ns).
 uint64_t pipeline_wait_limit_ns();

@@ -18,6 +18,7 @@
 // with the same inputs.
 #include <algorithm>
 #include <atomic>
+#include <cstdlib>
 
 #include "epoch_body.cuh"
 
@@ -64,11 +65,6 @@ __global__ void mutation_mask_kernel(uint64_t s0, uint64_t e0, uint64_t npairs, 
 }
 
 constexpr int kCountSlots = kPipeCountSlots;  // per-epoch counter slots (spread the atomics)
-// Interpreter steps a running lane takes per iteration of its warp.  The same
-// count for every lane: an iteration lasts as long as its busiest lane, so a
-// lane given more steps than its warp-mates holds them all (and the pairs
-// they would finish and notify) for its extra steps.
-constexpr int kStepsPerVisit = 64;
 
 // Ready-queue dataflow over one or more soups.  A pair of epoch e+1 can run
 // once the two pairs of epoch e that wrote its programs are done.  A finished
@@ -90,11 +86,21 @@ constexpr int kStepsPerVisit = 64;
 // registers read back in a later iteration.  Lane states:
 //   idle -> slot (wait for the entry) -> index -> stage -> run -> notify -> idle
 // and `exhausted` once a claim falls past the queue's last task.
-// A warp with running lanes claims new slots only once at least kClaimMin of
-// its lanes are idle (an idle warp claims at once): a slot held by a busy
-// warp is polled only between its long iterations, so claims are left to
-// warps with many free lanes.  Swept 4-32 on the single soup and the mix.
-constexpr int kClaimMin = 20;
+//
+// Launch-shape knobs (PipeTuning, chosen by the host):
+//  * steps_per_visit: interpreter steps a running lane takes per iteration of
+//    its warp, the same for every lane (an iteration lasts as long as its
+//    busiest lane, so a lane given more steps holds its warp-mates, and the
+//    pairs they would finish and notify, for its extra steps);
+//  * claim_min: a warp with running lanes claims new slots only once this
+//    many of its lanes are idle (an idle warp claims at once), so a slot held
+//    by a busy warp is polled only between its long iterations;
+//  * long_visits: a pair still running after this many visits is long.  A
+//    warp holding a long pair claims nothing new: its other lanes drain, and
+//    the long pair, which the next epochs' pairs wait on, steps without
+//    warp-mates whose staging and steps would interleave with its own.  Few
+//    pairs are long (a random 2^17-program soup has ~10-25 pairs per epoch
+//    past 64 steps, out of 65536), so little capacity is set aside.
 
 __device__ __forceinline__ uint32_t atom_add_acq_rel(uint32_t *p, uint32_t v) {
   uint32_t old;
@@ -110,7 +116,7 @@ enum : uint32_t { kIdle, kSlot, kIndex, kStage, kRun, kNotify, kExhausted };
 
 // Per-lane state that does not depend on the language.
 struct Lane {
-  uint32_t state, slot, task, e, k, p1, p2, qv, poll_gap, poll_in, err, j1, j2, c1, c2;
+  uint32_t state, slot, task, e, k, p1, p2, qv, poll_gap, poll_in, err, j1, j2, c1, c2, visits;
   int si;  // soup index of the task
   uint64_t qp, t_wait;
   bool dirty, evaluated, has_next;
@@ -124,6 +130,7 @@ struct PipeCtx {
   const PipeSoup *soups;
   int *error;
   uint64_t wait_limit_ns;
+  PipeTuning tune;
 };
 
 // Soup of global task `task` among soups [lo, hi) (sorted by task_base).
@@ -159,7 +166,8 @@ __device__ __forceinline__ bool iterate(const PipeCtx &b, const PipeQueue &q, La
   // 1. Bulk claim of queue slots by idle lanes.
   const uint32_t idle = __ballot_sync(0xffffffffu, ln.state == kIdle);
   const uint32_t busy = __ballot_sync(0xffffffffu, ln.state != kIdle && ln.state != kExhausted);
-  if (idle && (__popc(idle) >= kClaimMin || busy == 0)) {
+  const uint32_t lng = __ballot_sync(0xffffffffu, ln.state == kRun && ln.visits >= b.tune.long_visits);
+  if (idle && (busy == 0 || (lng == 0 && __popc(idle) >= b.tune.claim_min))) {
     const int leader = __ffs(idle) - 1;
     uint32_t base = 0;
     if (lane == static_cast<uint32_t>(leader)) base = atomicAdd(q.ctl, __popc(idle));
@@ -289,13 +297,15 @@ __device__ __forceinline__ bool iterate(const PipeCtx &b, const PipeQueue &q, La
     const uint64_t num_indices = sp.num_indices ? sp.num_indices[ln.e] : sp.npairs;
     ln.evaluated = ln.k < num_indices;
     m.begin(t, cmd);
+    ln.visits = 0;
     ln.state = kRun;
     progressed = true;
   } else if (ln.state == kRun) {
     // 5. A few interpreter steps; on the end, write back and notify.
     progressed = true;
     bool fin = !ln.evaluated;
-    for (int r = 0; r < kStepsPerVisit && !fin; r++) fin = m.step(t, stk, np, optab);
+    for (uint32_t r = 0; r < b.tune.steps_per_visit && !fin; r++) fin = m.step(t, stk, np, optab);
+    ln.visits++;
     if (fin) {
       const PipeSoup &sp = b.soups[ln.si];
       if (ln.dirty || (ln.evaluated && m.mods() != 0)) {
@@ -365,7 +375,7 @@ __device__ __forceinline__ void serve(const PipeCtx &b, const PipeQueue &q,
   ln.state = kIdle;
   ln.slot = ln.task = ln.e = ln.k = ln.p1 = ln.p2 = ln.qv = 0;
   ln.poll_gap = 1;
-  ln.poll_in = ln.err = ln.j1 = ln.j2 = ln.c1 = ln.c2 = 0;
+  ln.poll_in = ln.err = ln.j1 = ln.j2 = ln.c1 = ln.c2 = ln.visits = 0;
   ln.si = 0;
   ln.qp = ln.t_wait = 0;
   ln.dirty = ln.evaluated = ln.has_next = false;
@@ -421,7 +431,7 @@ __global__ void __launch_bounds__(kThreads, (L <= kBffSelfmove) ? 3 : 4)
   const LaneBytes stk{smem + kGroups * kGroupBytes, lane_base(tid)};
   const uint32_t warp = blockIdx.x * (kThreads / 32) + (tid >> 5);
   const LaneNp np{L <= kBffSelfmove ? npa : nullptr, tid};
-  const PipeCtx b{soups, pb.error, pb.wait_limit_ns};
+  const PipeCtx b{soups, pb.error, pb.wait_limit_ns, pb.tune};
   const PipeQueue q = pb.queue;
   serve<L>(b, q, optab, cmdflag, t, stk, np, lane, warp % kCountSlots);
 }
@@ -460,6 +470,36 @@ int launch_pipeline_t(const PipeBatch &b, uint64_t total_pairs, uint32_t lanes_p
 }  // namespace
 
 uint64_t pipeline_wait_limit_ns() { return g_wait_limit_ns.load(); }
+
+namespace {
+uint32_t env_u32(const char *name, uint32_t dflt, uint32_t lo, uint32_t hi) {
+  const char *v = std::getenv(name);
+  if (!v || !*v) return dflt;
+  const long x = std::strtol(v, nullptr, 10);
+  return x < long(lo) ? lo : x > long(hi) ? hi : static_cast<uint32_t>(x);
+}
+}  // namespace
+
+// Default launch shape: half an epoch of pairs in flight, 64 steps per visit,
+// claims by warps with at least 20 idle lanes, pairs past their first visit
+// kept without new warp-mates.
+cubff_tuning default_shape() {
+  static const cubff_tuning t = {env_u32("CUBFF_LANES_PER_PAIR64", 32, 1, 64),
+                                 env_u32("CUBFF_STEPS_PER_VISIT", 64, 1, 4096),
+                                 env_u32("CUBFF_CLAIM_MIN", 20, 1, 32),
+                                 env_u32("CUBFF_LONG_VISITS", 1, 0, 1u << 20)};
+  return t;
+}
+
+bool valid_shape(const cubff_tuning &t) {
+  return t.lanes_per_pair64 >= 1 && t.lanes_per_pair64 <= 64 && t.steps_per_visit >= 1 &&
+         t.steps_per_visit <= 4096 && t.claim_min >= 1 && t.claim_min <= 32;
+}
+
+PipeTuning pipe_tuning(const cubff_tuning &t) {
+  return PipeTuning{t.steps_per_visit, t.claim_min,
+                    t.long_visits ? t.long_visits : 0xffffffffu};
+}
 
 int launch_pipeline(const PipeBatch &b, uint64_t total_pairs, uint32_t lanes_per_pair64,
                     int device, cudaStream_t stream) {
@@ -562,7 +602,25 @@ extern "C" int cubff_run_epochs(int lang, uint8_t *d_programs, const uint32_t *d
                                 uint64_t first_epoch, uint32_t n_epochs, uint32_t mutation_prob,
                                 uint64_t num_programs, unsigned long long *d_counts,
                                 void *d_workspace, size_t workspace_bytes, void *stream) {
+  return cubff_run_epochs_tuned(lang, d_programs, d_shuf_idx, d_num_indices, params_seed,
+                                first_epoch, n_epochs, mutation_prob, num_programs, d_counts,
+                                d_workspace, workspace_bytes, nullptr, stream);
+}
+
+extern "C" void cubff_default_tuning(cubff_tuning *out) {
+  if (out) *out = cubff::default_shape();
+}
+
+extern "C" int cubff_run_epochs_tuned(int lang, uint8_t *d_programs, const uint32_t *d_shuf_idx,
+                                      const uint64_t *d_num_indices, uint64_t params_seed,
+                                      uint64_t first_epoch, uint32_t n_epochs,
+                                      uint32_t mutation_prob, uint64_t num_programs,
+                                      unsigned long long *d_counts, void *d_workspace,
+                                      size_t workspace_bytes, const cubff_tuning *tuning,
+                                      void *stream) {
   using namespace cubff;
+  const cubff_tuning shape = tuning ? *tuning : default_shape();
+  if (!valid_shape(shape)) return set_error(CUBFF_EINVAL, "run_epochs: launch shape out of range");
   if (lang < 0 || lang >= kNumLangs) return set_error(CUBFF_ENOTFOUND, "unknown language %d", lang);
   if (!d_programs || !d_shuf_idx || !d_counts || !d_workspace || num_programs < 2 ||
       num_programs % 2 != 0 || num_programs > (1ull << 31))
@@ -618,7 +676,8 @@ extern "C" int cubff_run_epochs(int lang, uint8_t *d_programs, const uint32_t *d
   b.n_soups = 1;
   b.error = reinterpret_cast<int *>(w.ctl + 2);
   b.wait_limit_ns = pipeline_wait_limit_ns();
-  CUBFF_TRY(launch_pipeline(b, P, 0, dev, st));
+  b.tune = pipe_tuning(shape);
+  CUBFF_TRY(launch_pipeline(b, P, shape.lanes_per_pair64, dev, st));
   reduce_counts_kernel<<<(n_epochs + 127) / 128, 128, 0, st>>>(w.counters, n_epochs, d_counts);
   CUBFF_CUDA_TRY(cudaGetLastError());
   return CUBFF_OK;

@@ -5,9 +5,9 @@
 //   1. admits queued jobs in submission order while the running jobs'
 //      summed footprint stays within the budget (the head of the queue is
 //      never skipped, so a large job cannot starve),
-//   2. advances every running job by min(round_epochs, the smallest number
-//      of epochs a running job has left) epochs in one run_soups call
-//      (pipelined launches shared by all running jobs),
+//   2. advances every running job by min(round_epochs, the epochs it has
+//      left) in one run_soups call (pipelined launches shared by all running
+//      jobs; a job near its end does not shorten the others' round),
 //   3. retires the jobs that are done: soup bytes and op counts to the host,
 //      device memory released.
 // A job's results equal cubff_soup_run's for the same parameters: run_soups
@@ -124,23 +124,26 @@ void cubff_server::loop() {
       std::this_thread::sleep_for(std::chrono::milliseconds(1));
       continue;
     }
-    uint64_t quantum = round_epochs;
-    for (auto &j : running) quantum = std::min(quantum, j->n_epochs - j->done);
+    // Every job advances by its own quantum: round_epochs, or what it has
+    // left (a job about to finish does not shorten the others' round).
     std::vector<cubff_soup *> soups;
     std::vector<uint64_t *> ops;
+    std::vector<uint64_t> quantum;
     for (auto &j : running) {
       soups.push_back(j->soup);
       ops.push_back(j->ops.data() + j->done);
+      quantum.push_back(std::min<uint64_t>(round_epochs, j->n_epochs - j->done));
     }
-    const int st = cubff::run_soups(eng, soups.data(), static_cast<int>(soups.size()), quantum,
-                                    ops.data(), nullptr, nullptr);
+    const int st = cubff::run_soups(eng, soups.data(), static_cast<int>(soups.size()), round_epochs,
+                                    ops.data(), nullptr, nullptr, quantum.data());
     std::vector<std::unique_ptr<Job>> keep;
-    for (auto &j : running) {
+    for (size_t q = 0; q < running.size(); q++) {
+      auto &j = running[q];
       if (st != CUBFF_OK) {
         retire(std::move(j), st);
         continue;
       }
-      j->done += quantum;
+      j->done += quantum[q];
       if (j->done == j->n_epochs) retire(std::move(j), CUBFF_OK);
       else keep.push_back(std::move(j));
     }

@@ -116,6 +116,20 @@ int cubff_shuffle_indices(uint64_t params_seed, uint64_t first_epoch,
  * Asynchronous; cubff_run_epochs_status synchronizes the stream and reports
  * CUBFF_ETIMEDOUT if a bounded wait inside the launch gave up.  Results are
  * identical to the per-epoch launches. */
+/* Launch shape of a pipelined launch.  Results never depend on it; only the
+ * time does.  Chosen per launch group by the engine's tuner
+ * (cubff_engine_tune), or set by hand. */
+typedef struct {
+  uint32_t lanes_per_pair64; /* lanes in flight per 64 pairs of an epoch (grid size)    */
+  uint32_t steps_per_visit;  /* interpreter steps a lane takes per iteration of its warp */
+  uint32_t claim_min;        /* idle lanes a busy warp needs before it claims new pairs   */
+  uint32_t long_visits;      /* a pair running longer than this many visits keeps its
+                                warp from claiming (0 = never)                            */
+} cubff_tuning;
+
+/* The default launch shape (what a launch uses without a tuned one). */
+void cubff_default_tuning(cubff_tuning *out);
+
 size_t cubff_run_epochs_workspace_bytes(uint64_t num_programs, uint32_t n_epochs);
 int cubff_run_epochs(int lang, uint8_t *d_programs, const uint32_t *d_shuf_idx,
                      const uint64_t *d_num_indices, uint64_t params_seed,
@@ -124,6 +138,13 @@ int cubff_run_epochs(int lang, uint8_t *d_programs, const uint32_t *d_shuf_idx,
                      void *d_workspace, size_t workspace_bytes, void *stream);
 int cubff_run_epochs_status(const void *d_workspace, uint64_t num_programs,
                             uint32_t n_epochs, void *stream);
+/* cubff_run_epochs with an explicit launch shape (tuning; NULL = default). */
+int cubff_run_epochs_tuned(int lang, uint8_t *d_programs, const uint32_t *d_shuf_idx,
+                           const uint64_t *d_num_indices, uint64_t params_seed,
+                           uint64_t first_epoch, uint32_t n_epochs, uint32_t mutation_prob,
+                           uint64_t num_programs, unsigned long long *d_counts,
+                           void *d_workspace, size_t workspace_bytes,
+                           const cubff_tuning *tuning, void *stream);
 
 /* Bound of the waits inside pipelined launches (cubff_run_epochs, soup runs,
  * batches, the server): a lane waiting longer than ns nanoseconds for a
@@ -148,6 +169,13 @@ int cubff_set_wait_limit_ns(uint64_t ns, uint64_t *previous);
 int cubff_shuffle_indices_noalloc(uint64_t params_seed, uint64_t first_epoch,
                                   uint32_t n_epochs, uint64_t num_programs,
                                   uint32_t *d_out, void *stream);
+
+/* Measured integer-instruction rate of a device, in lane-instructions per
+ * second (one lane retiring one 32-bit integer instruction counts 1): alu =
+ * chains of adds and xors, mixed = the same plus an integer multiply-add per
+ * link.  The roofline denominator of the interpreters (which are integer
+ * code); no reference counterpart.  Runs two short kernels (~0.1 s). */
+int cubff_measure_int_issue(int device, double *alu_per_s, double *mixed_per_s);
 
 /* ---- layer 2: device-resident soups ------------------------------------ */
 typedef struct cubff_engine cubff_engine;
@@ -233,6 +261,31 @@ int cubff_eval_selfrep(int lang, const uint8_t *program, uint64_t epoch_key,
  * soup, its cached pairings (perm, inverse, mutation masks, ready counters),
  * pairing scratch, op counters and its share of the ready queue. */
 uint64_t cubff_soup_footprint_bytes(const cubff_soup_params *params);
+
+/* ---- launch-shape tuner ------------------------------------------------- */
+/* The reference launches ceil(N/64) blocks of 32 threads, one thread per
+ * pair, for every language and size (common_language.h:348, :490-493).  Here
+ * the launch shape of a pipelined launch (cubff_tuning) is picked per launch
+ * group, keyed by (language, log2 of the group's programs, log2 of its soup
+ * count): the engine keeps a cache of tuned shapes and uses the default for
+ * keys it has not tuned.
+ *
+ * cubff_engine_tune runs trial_epochs epochs of copies of the given soups
+ * (their current bytes and epoch; the soups themselves are not advanced)
+ * under candidate shapes, by coordinate descent over the four knobs from the
+ * default, checks that every candidate gives the same op counts, and caches
+ * the fastest shape for each launch group the soups form.  chosen (nullable,
+ * n_soups entries) receives the shape that now applies to each soup.
+ * trial_epochs = 0 picks 16. */
+int cubff_engine_tune(cubff_engine *engine, cubff_soup **soups, int n_soups,
+                      uint32_t trial_epochs, cubff_tuning *chosen);
+/* The cached shape for a launch group of `lang` holding `group_programs`
+ * programs in `group_soups` soups (the default when none is cached), and
+ * setting it by hand. */
+int cubff_engine_get_tuning(cubff_engine *engine, int lang, uint64_t group_programs,
+                            uint32_t group_soups, cubff_tuning *out);
+int cubff_engine_set_tuning(cubff_engine *engine, int lang, uint64_t group_programs,
+                            uint32_t group_soups, const cubff_tuning *tuning);
 
 /* ---- layer 3: batching ------------------------------------------------- */
 /* Advances every soup by n_epochs epochs, as cubff_soup_run does for each

@@ -206,9 +206,9 @@ def main(argv):
                        "source": "reference CPU build (oracle/_ref/cubff)", "runs": out},
                       f, indent=0)
     elif mode in ("c2", "c3", "c4", "c5"):
-        # Full-size configurations: hash and op delta every 256 epochs (the
-        # callback fires after 0-based epochs 0, 256, 512, ...; a run stops at
-        # the first callback at or past its epoch count).
+        # Full-size configurations: hash and op delta at every callback (it
+        # fires after 0-based epochs 0, ci, 2 ci, ...; a run stops at the
+        # first callback at or past its epoch count).
         path = os.path.join(HERE, f"ref_{mode}.json")
         out = json.load(open(path))["runs"] if os.path.exists(path) else {}
         for spec in config_specs(mode):
@@ -240,9 +240,10 @@ def config_specs(mode: str):
                       "pattern": {"grid": [512, 256], "radius": 2}})
         return specs
     if mode == "c4":
+        # Callbacks every 89 epochs end exactly at epoch 2048 (2047 = 89 * 23).
         return [{"name": f"c4_{s.seed}", "lang": s.lang, "num_programs": s.num_programs,
                  "seed": s.seed, "mutation_prob": s.mutation_prob, "epochs": s.epochs,
-                 "callback_interval": 256} for s in workloads.batch_mix(2048)]
+                 "callback_interval": 89} for s in workloads.batch_mix(2048)]
     if mode == "c5":
         # Every job's result is compared on the GPU alone and in the mix; this
         # seeded sample of the 2000 jobs is also checked against the reference.

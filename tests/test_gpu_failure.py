@@ -90,6 +90,8 @@ def test_batch_run_times_out_then_runs_exactly():
         want_ops, want_soup = _oracle(lang, n, seed, 30)
         assert got[i].tolist() == want_ops
         assert np.array_equal(soups[i].read(), want_soup)
+    for s in soups:
+        s.close()
     eng.close()
 
 
