@@ -283,7 +283,7 @@ int run_soups(cubff_engine *eng, cubff_soup *const *soups, int n_soups, uint64_t
         p.seg = static_cast<uint32_t>(seg);
         if (ni && ni[i]) {
           for (uint64_t q = 0; q < seg; q++)
-            ni[i][p.done + q] = s->p.pairing == CUBFF_PAIR_PATTERN ? s->pat_ni[slot + q] : P;
+            ni[i][p.done + q] = s->p.pairing == CUBFF_PAIR_PATTERN ? s->h_pat_ni[slot + q] : P;
         }
       }
       if (pb.n_soups == 0) continue;
@@ -302,15 +302,6 @@ int run_soups(cubff_engine *eng, cubff_soup *const *soups, int n_soups, uint64_t
       pb.tune = pipe_tuning(shape);
       CUBFF_CUDA_TRY(cudaMemsetAsync(q.ctl, 0, 2 * sizeof(uint32_t), g.st));  // head, tail
       CUBFF_TRY(launch_pipeline(pb, pairs, shape.lanes_per_pair64, eng->device, g.st));
-      // Pattern pairings are built on the host: build the next batch of a
-      // soup whose run goes on past its cached one while this launch runs.
-      for (int i : g.members) {
-        cubff_soup *s = soups[i];
-        if (s->p.pairing != CUBFF_PAIR_PATTERN || pr[i].seg == 0) continue;
-        const uint64_t next = s->perm_first + s->perm_count, end = s->epoch + want(i);
-        if (next < end && !(s->pat_worker.joinable() && s->pat_pf_first == next))
-          CUBFF_TRY(s->prefetch_pattern(next, static_cast<uint32_t>(std::min<uint64_t>(s->batch, end - next))));
-      }
       for (int i : g.members) {
         cubff_soup *s = soups[i];
         Progress &p = pr[i];

@@ -8,7 +8,6 @@
 #include <cstring>
 #include <mutex>
 #include <string>
-#include <thread>
 #include <vector>
 
 #include "common.cuh"
@@ -43,42 +42,6 @@ const char *const kLangNames[kNumLangs] = {
 
 }  // namespace
 
-// ---------------------------------------------------------------------------
-// Host pattern pairing (common_language.h:435-463): serial Fisher-Yates of
-// 0..n-1, then greedy matching in that order, program i proposing neighbour
-// list_i[seed(seed(epoch) ^ seed(i)) % |list_i|].  Unused programs follow in
-// increasing order.  Returns num_indices.
-uint64_t pattern_pairing_host(uint64_t s0, uint64_t epoch, uint64_t n,
-                              const uint32_t *offs, const uint32_t *tgts,
-                              uint32_t *s, std::vector<uint32_t> &order,
-                              std::vector<uint8_t> &used) {
-  order.resize(n);
-  used.assign(n, 0);
-  for (uint64_t i = 0; i < n; i++) order[i] = static_cast<uint32_t>(i);
-  for (uint64_t i = n; i-- > 0;) {
-    const uint64_t j = splitmix64(seed_from(s0, epoch * n + i)) % (i + 1);
-    std::swap(order[i], order[j]);
-  }
-  const uint64_t ek = seed_from(s0, epoch);
-  uint64_t num = 0;
-  for (uint64_t t = 0; t < n; t++) {
-    const uint32_t i = order[t];
-    const uint64_t len = offs[i + 1] - offs[i];
-    if (len == 0) continue;
-    const uint64_t pick = seed_from(s0, ek ^ seed_from(s0, i)) % len;
-    const uint32_t nb = tgts[offs[i] + pick];
-    if (used[i] || used[nb]) continue;
-    used[i] = used[nb] = 1;
-    s[2 * num] = i;
-    s[2 * num + 1] = nb;
-    num++;
-  }
-  uint64_t idx = 2 * num;
-  for (uint64_t i = 0; i < n; i++)
-    if (!used[i]) s[idx++] = static_cast<uint32_t>(i);
-  return num;
-}
-
 }  // namespace cubff
 
 using namespace cubff;
@@ -103,9 +66,14 @@ int cubff_soup::ensure_buffers() {
     batch = pairing_batch(p.num_programs);
     CUBFF_CUDA_TRY(cudaMalloc(&d_perm, size_t(batch) * p.num_programs * sizeof(uint32_t)));
     CUBFF_CUDA_TRY(cudaMalloc(&d_num_indices, size_t(batch) * sizeof(uint64_t)));
-    if (p.pairing == CUBFF_PAIR_SHUFFLE) {
-      scratch_bytes = shuffle_scratch_bytes(p.num_programs, batch);
+    if (p.pairing == CUBFF_PAIR_SHUFFLE || p.pairing == CUBFF_PAIR_PATTERN) {
+      scratch_bytes = p.pairing == CUBFF_PAIR_SHUFFLE ? shuffle_scratch_bytes(p.num_programs, batch)
+                                                      : pattern_scratch_bytes(p.num_programs, batch);
       CUBFF_CUDA_TRY(cudaMalloc(&d_scratch, scratch_bytes));
+    }
+    if (p.pairing == CUBFF_PAIR_PATTERN) {
+      CUBFF_CUDA_TRY(cudaMallocHost(&h_pat_ni, size_t(batch) * sizeof(uint64_t)));
+      CUBFF_CUDA_TRY(cudaMallocHost(&h_pat_undecided, size_t(batch) * sizeof(uint32_t)));
     }
     CUBFF_CUDA_TRY(cudaMalloc(&d_counters, kCounterWords * sizeof(unsigned long long)));
     CUBFF_CUDA_TRY(cudaMallocHost(&h_counters, kCounterWords * sizeof(unsigned long long)));
@@ -131,13 +99,13 @@ void cubff_soup::release() {
   if (d_scratch) cudaFree(d_scratch);
   if (d_counters) cudaFree(d_counters);
   if (h_counters) cudaFreeHost(h_counters);
-  drop_pattern_prefetch();
-  if (h_pat_perm) cudaFreeHost(h_pat_perm);
-  if (h_pat_perm2) cudaFreeHost(h_pat_perm2);
-  if (pat_up) cudaEventDestroy(pat_up);
-  if (pat_up2) cudaEventDestroy(pat_up2);
-  h_pat_perm2 = nullptr;
-  pat_up = pat_up2 = nullptr;
+  if (d_pat_offs) cudaFree(d_pat_offs);
+  if (d_pat_tgts) cudaFree(d_pat_tgts);
+  if (h_pat_ni) cudaFreeHost(h_pat_ni);
+  if (h_pat_undecided) cudaFreeHost(h_pat_undecided);
+  d_pat_offs = d_pat_tgts = nullptr;
+  h_pat_ni = nullptr;
+  h_pat_undecided = nullptr;
   if (d_inv) cudaFree(d_inv);
   if (d_readycnt) cudaFree(d_readycnt);
   d_inv = d_readycnt = nullptr;
@@ -149,7 +117,6 @@ void cubff_soup::release() {
   d_scratch = nullptr;
   d_counters = nullptr;
   h_counters = nullptr;
-  h_pat_perm = nullptr;
 }
 
 // Computes the pairing of epochs [first, first + count) into d_perm.
@@ -165,39 +132,15 @@ int cubff_soup::fill_pairing(uint64_t first, uint32_t count, cudaStream_t st) {
     case CUBFF_PAIR_CYCLIC:
       CUBFF_TRY(launch_cyclic(first, count, n, d_perm, st));
       break;
-    case CUBFF_PAIR_PATTERN: {
-      if (pat_offs.empty())
+    case CUBFF_PAIR_PATTERN:
+      if (!d_pat_offs)
         return set_error(CUBFF_EINVAL, "pattern pairing without interaction lists");
-      if (!h_pat_perm) {
-        CUBFF_CUDA_TRY(cudaMallocHost(&h_pat_perm, (size_t(batch) * n + batch) * sizeof(uint64_t)));
-        CUBFF_CUDA_TRY(cudaEventCreateWithFlags(&pat_up, cudaEventDisableTiming));
-      }
-      bool have = false;
-      if (pat_worker.joinable()) {  // built ahead while the previous batch ran
-        pat_worker.join();
-        if (pat_pf_ok && pat_pf_first == first && pat_pf_count == count) {
-          std::swap(h_pat_perm, h_pat_perm2);
-          std::swap(pat_up, pat_up2);
-          have = true;
-        }
-        pat_pf_count = 0;
-      }
-      if (!have) {
-        // The last upload from this buffer must have finished before it is
-        // rewritten.
-        CUBFF_CUDA_TRY(cudaEventSynchronize(pat_up));
-        compute_pattern(first, count, h_pat_perm);
-      }
-      uint32_t *hp = reinterpret_cast<uint32_t *>(h_pat_perm);
-      uint64_t *hn = h_pat_perm + (size_t(batch) * n + 1) / 2;
-      pat_ni.assign(hn, hn + count);
-      CUBFF_CUDA_TRY(cudaMemcpyAsync(d_perm, hp, size_t(count) * n * sizeof(uint32_t),
-                                     cudaMemcpyHostToDevice, st));
-      CUBFF_CUDA_TRY(cudaMemcpyAsync(d_num_indices, hn, size_t(count) * sizeof(uint64_t),
-                                     cudaMemcpyHostToDevice, st));
-      CUBFF_CUDA_TRY(cudaEventRecord(pat_up, st));
+      CUBFF_TRY(launch_pattern(s0, first, count, n, d_pat_offs, d_pat_tgts, d_perm, d_num_indices,
+                               d_scratch, h_pat_undecided, st));
+      CUBFF_CUDA_TRY(cudaMemcpyAsync(h_pat_ni, d_num_indices, size_t(count) * sizeof(uint64_t),
+                                     cudaMemcpyDeviceToHost, st));
+      CUBFF_CUDA_TRY(cudaStreamSynchronize(st));
       break;
-    }
     default:
       return set_error(CUBFF_EINVAL, "unknown pairing mode %d", p.pairing);
   }
@@ -206,55 +149,6 @@ int cubff_soup::fill_pairing(uint64_t first, uint32_t count, cudaStream_t st) {
   perm_first = first;
   perm_count = count;
   return CUBFF_OK;
-}
-
-// Pattern pairings of epochs [first, first + count) into a staging buffer
-// (batch * n shuffle entries, then the epochs' num_indices), on host threads.
-void cubff_soup::compute_pattern(uint64_t first, uint32_t count, uint64_t *buf) {
-  const uint64_t n = p.num_programs;
-  uint32_t *hp = reinterpret_cast<uint32_t *>(buf);
-  uint64_t *hn = buf + (size_t(batch) * n + 1) / 2;
-  const unsigned hw = std::max(1u, std::min<unsigned>(std::thread::hardware_concurrency(), count));
-  std::vector<std::thread> pool;
-  for (unsigned w = 0; w < hw; w++) {
-    pool.emplace_back([&, w] {
-      std::vector<uint32_t> order;
-      std::vector<uint8_t> used;
-      for (uint32_t e = w; e < count; e += hw)
-        hn[e] = pattern_pairing_host(s0, first + e, n, pat_offs.data(), pat_tgts.data(),
-                                     hp + size_t(e) * n, order, used);
-    });
-  }
-  for (auto &t : pool) t.join();
-}
-
-// Starts building the pattern pairings of [first, first + count) on a host
-// thread, into the second staging buffer once its last upload has finished;
-// fill_pairing takes them when it gets to `first`.
-int cubff_soup::prefetch_pattern(uint64_t first, uint32_t count) {
-  drop_pattern_prefetch();
-  const uint64_t n = p.num_programs;
-  if (!h_pat_perm2) {
-    CUBFF_CUDA_TRY(cudaMallocHost(&h_pat_perm2, (size_t(batch) * n + batch) * sizeof(uint64_t)));
-    CUBFF_CUDA_TRY(cudaEventCreateWithFlags(&pat_up2, cudaEventDisableTiming));
-  }
-  pat_pf_first = first;
-  pat_pf_count = count;
-  pat_pf_ok = false;
-  const int device = eng->device;
-  pat_worker = std::thread([this, first, count, device] {
-    cudaSetDevice(device);
-    if (cudaEventSynchronize(pat_up2) != cudaSuccess) return;
-    compute_pattern(first, count, h_pat_perm2);
-    pat_pf_ok = true;
-  });
-  return CUBFF_OK;
-}
-
-void cubff_soup::drop_pattern_prefetch() {
-  if (pat_worker.joinable()) pat_worker.join();
-  pat_pf_count = 0;
-  pat_pf_ok = false;
 }
 
 int cubff_soup::apply_reset(cudaStream_t st) {
@@ -425,6 +319,7 @@ uint64_t cubff_soup_footprint_bytes(const cubff_soup_params *params) {
   uint64_t bytes = n * kTape;                                     // the soup
   bytes += batch * n * sizeof(uint32_t) + batch * sizeof(uint64_t);  // pairings, num_indices
   if (params->pairing == CUBFF_PAIR_SHUFFLE) bytes += shuffle_scratch_bytes(n, batch);
+  if (params->pairing == CUBFF_PAIR_PATTERN) bytes += pattern_scratch_bytes(n, batch);
   bytes += kCounterWords * sizeof(unsigned long long);            // op counters
   bytes += batch * P * sizeof(uint4);                             // mutation masks
   bytes += batch * n * sizeof(uint32_t);                          // inverse shuffles
@@ -458,7 +353,16 @@ int cubff_soup_set_pattern(cubff_soup *soup, const uint32_t *offs, const uint32_
                          static_cast<unsigned long long>(i));
     }
   }
-  soup->drop_pattern_prefetch();  // built from the previous lists
+  CUBFF_CUDA_TRY(cudaSetDevice(soup->eng->device));
+  CUBFF_CUDA_TRY(cudaStreamSynchronize(soup->eng->stream));  // lists in use by earlier work
+  if (soup->d_pat_offs) cudaFree(soup->d_pat_offs);
+  if (soup->d_pat_tgts) cudaFree(soup->d_pat_tgts);
+  soup->d_pat_offs = soup->d_pat_tgts = nullptr;
+  CUBFF_CUDA_TRY(cudaMalloc(&soup->d_pat_offs, (n + 1) * sizeof(uint32_t)));
+  CUBFF_CUDA_TRY(cudaMalloc(&soup->d_pat_tgts, std::max<uint64_t>(ne, 1) * sizeof(uint32_t)));
+  CUBFF_CUDA_TRY(cudaMemcpy(soup->d_pat_offs, offs, (n + 1) * sizeof(uint32_t), cudaMemcpyHostToDevice));
+  if (ne)
+    CUBFF_CUDA_TRY(cudaMemcpy(soup->d_pat_tgts, tgts, ne * sizeof(uint32_t), cudaMemcpyHostToDevice));
   soup->pat_offs.assign(offs, offs + n + 1);
   soup->pat_tgts.assign(tgts, tgts + ne);
   soup->perm_count = 0;  // cached pairings are stale

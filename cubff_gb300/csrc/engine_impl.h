@@ -3,7 +3,6 @@
 
 #include <cstdint>
 #include <map>
-#include <thread>
 #include <vector>
 
 #include <cuda_runtime.h>
@@ -55,17 +54,11 @@ struct cubff_soup {
   uint32_t perm_count = 0;
   void *d_scratch = nullptr;
   size_t scratch_bytes = 0;
-  uint64_t *h_pat_perm = nullptr;  // pinned staging for host pattern pairings
-  std::vector<uint64_t> pat_ni;    // num_indices of the cached pattern pairings
-  cudaEvent_t pat_up = nullptr;    // recorded after the last upload from h_pat_perm
-  // The next batch of pattern pairings, built by a host thread into a second
-  // staging buffer while the current batch runs on the device.
-  std::thread pat_worker;
-  uint64_t *h_pat_perm2 = nullptr;
-  cudaEvent_t pat_up2 = nullptr;
-  uint64_t pat_pf_first = 0;
-  uint32_t pat_pf_count = 0;
-  bool pat_pf_ok = false;
+  // Pattern pairing, built on the device: the interaction lists (CSR) and the
+  // num_indices of the cached pairings, copied back to pinned memory.
+  uint32_t *d_pat_offs = nullptr, *d_pat_tgts = nullptr;
+  uint64_t *h_pat_ni = nullptr;      // [batch] pinned
+  uint32_t *h_pat_undecided = nullptr;  // [batch] pinned (convergence checks)
 
   // Pipelined runs: inverse shuffles, mutation masks and ready counters of
   // the cached epochs (the counters are zero between launches).
@@ -86,9 +79,6 @@ struct cubff_soup {
   int ensure_buffers();
   void release();
   int fill_pairing(uint64_t first, uint32_t count, cudaStream_t st);
-  void compute_pattern(uint64_t first, uint32_t count, uint64_t *buf);
-  int prefetch_pattern(uint64_t first, uint32_t count);
-  void drop_pattern_prefetch();
   int apply_reset(cudaStream_t st);
 };
 

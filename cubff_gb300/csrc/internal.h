@@ -80,11 +80,12 @@ struct PipeTuning {
   uint32_t claim_min;        // idle lanes a busy warp needs before it claims new pairs
   uint32_t long_visits;      // visits after which a pair counts as long: its warp stops
                              // claiming, so the pair runs without new warp-mates
+  uint32_t first_visit_steps;  // steps of a pair's first visit
 };
 // The default launch shape (cubff_tuning: lanes in flight per 64 pairs, then
 // the PipeTuning knobs; long_visits 0 = never), each knob overridable by the
 // environment (CUBFF_LANES_PER_PAIR64, CUBFF_STEPS_PER_VISIT, CUBFF_CLAIM_MIN,
-// CUBFF_LONG_VISITS), read once.
+// CUBFF_LONG_VISITS, CUBFF_FIRST_VISIT_STEPS), read once.
 cubff_tuning default_shape();
 // The kernel's view of a shape; false when a knob is out of range.
 bool valid_shape(const cubff_tuning &t);
@@ -122,6 +123,15 @@ int launch_selfrep(int lang, const uint8_t *soup, uint64_t epoch_key,
 size_t shuffle_scratch_bytes(uint64_t n, uint32_t n_epochs);
 int launch_shuffle(uint64_t s0, uint64_t first_epoch, uint32_t n_epochs,
                    uint64_t n, uint32_t *out, void *scratch, cudaStream_t stream);
+// Pattern pairing (common_language.h:435-463) of n_epochs epochs on the
+// device: out[e] = the epoch's shuffle_idx, num_indices[e] its pair count.
+// Synchronises the stream (convergence checks read h_undecided, pinned,
+// n_epochs entries).
+size_t pattern_scratch_bytes(uint64_t n, uint32_t n_epochs);
+int launch_pattern(uint64_t s0, uint64_t first_epoch, uint32_t n_epochs, uint64_t n,
+                   const uint32_t *offs, const uint32_t *tgts, uint32_t *out,
+                   uint64_t *num_indices, void *scratch, uint32_t *h_undecided,
+                   cudaStream_t stream);
 int launch_fixed(uint64_t first_epoch, uint32_t n_epochs, uint64_t n,
                  uint32_t *out, cudaStream_t stream);
 int launch_cyclic(uint64_t first_epoch, uint32_t n_epochs, uint64_t n,

@@ -183,7 +183,213 @@ __global__ void inverse_kernel(const uint32_t *perm, uint64_t n, uint64_t m, uin
 
 unsigned blocks_for(uint64_t m, unsigned t) { return static_cast<unsigned>((m + t - 1) / t); }
 
+// ---------------------------------------------------------------------------
+// Pattern (2-D) pairing (common_language.h:435-463) on the device.
+//
+// The reference, on the host: take the Fisher-Yates order of 0..n-1 (the
+// draws of do_shuffle); for each i in that order with a non-empty list,
+// propose nb_i = list_i[seed(seed(epoch) ^ seed(i)) % |list_i|]; accept the
+// pair (i, nb_i) when neither i nor nb_i is used yet, and mark both.  Then
+// the unused programs follow in increasing order.
+//
+// That is greedy matching in a fixed priority order (the rank of i in the
+// order) over one proposal edge per program, and is rebuilt exactly in
+// parallel (greedy matching in rounds, Blelloch, Fineman and Shun, SPAA
+// 2012): edge e_i is accepted iff no edge of smaller rank that touches i or
+// nb_i is accepted.  The edges that can block e_i are e_{nb_i} and every e_j
+// with nb_j in {i, nb_i}; each round decides the undecided edges whose
+// blockers of smaller rank are all decided (one accepted blocker rejects at
+// once).  The smallest-rank undecided edge is always decidable, so rounds
+// end; with random ranks a few dozen suffice.  Accepted edges are then
+// written in rank order and unused programs in increasing order, both placed
+// by prefix sums.
+enum : uint8_t { kUndecided = 0, kAccepted = 1, kRejected = 2, kNoEdge = 3 };
+
+// nb[e][i] (or -1 for an empty list), and the in-degree counts for the
+// in-lists (cnt[e][v] += 1 for nb = v).
+__global__ void pat_propose(uint64_t s0, uint64_t first_epoch, uint64_t n, uint64_t m,
+                            const uint32_t *offs, const uint32_t *tgts, int32_t *nb,
+                            uint32_t *cnt, uint8_t *status) {
+  const uint64_t idx = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (idx >= m) return;
+  const uint64_t e = idx / n, i = idx - e * n;
+  const uint32_t lo = offs[i], len = offs[i + 1] - lo;
+  if (len == 0) {
+    nb[idx] = -1;
+    status[idx] = kNoEdge;
+    return;
+  }
+  const uint64_t ek = seed_from(s0, first_epoch + e);
+  const uint32_t v = tgts[lo + seed_from(s0, ek ^ seed_from(s0, i)) % len];
+  nb[idx] = static_cast<int32_t>(v);
+  status[idx] = kUndecided;
+  atomicAdd(&cnt[e * n + v], 1u);
+}
+
+// bucket[e][start[v] ..] = the programs j with nb_j = v.
+__global__ void pat_fill(uint64_t n, uint64_t m, const int32_t *nb, uint32_t *cnt,
+                         const uint32_t *start, uint32_t *bucket) {
+  const uint64_t idx = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (idx >= m || nb[idx] < 0) return;
+  const uint64_t e = idx / n, i = idx - e * n;
+  const uint64_t g = e * n + static_cast<uint32_t>(nb[idx]);
+  bucket[e * n + start[g] + atomicAdd(&cnt[g], 1u)] = static_cast<uint32_t>(i);
+}
+
+// One round over the undecided edges (statuses only move from undecided to
+// final, so reading a neighbour's status from this same round is safe).
+__global__ void pat_round(uint64_t n, uint64_t m, const int32_t *nb, const uint32_t *rank,
+                          const uint32_t *start, const uint32_t *len, const uint32_t *bucket,
+                          uint8_t *status, uint32_t *undecided) {
+  const uint64_t idx = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (idx >= m) return;
+  if (static_cast<volatile uint8_t *>(status)[idx] != kUndecided) return;
+  const uint64_t e = idx / n, i = idx - e * n, base = e * n;
+  const volatile uint8_t *st = status + base;
+  const uint32_t r = rank[idx];
+  const uint32_t b = static_cast<uint32_t>(nb[idx]);
+  bool all_decided = true;
+  // e_b, the edge proposed by the neighbour.
+  if (rank[base + b] < r) {
+    const uint8_t x = st[b];
+    if (x == kAccepted) {
+      status[idx] = kRejected;
+      return;
+    }
+    all_decided &= x != kUndecided;
+  }
+  // Every e_j with nb_j = i or nb_j = b (e_i itself among the latter).
+  for (int side = 0; side < 2; side++) {
+    const uint32_t v = side ? b : static_cast<uint32_t>(i);
+    const uint32_t s = start[base + v], l = len[base + v];
+    for (uint32_t q = 0; q < l; q++) {
+      const uint32_t j = bucket[base + s + q];
+      if (j == i || rank[base + j] >= r) continue;
+      const uint8_t x = st[j];
+      if (x == kAccepted) {
+        status[idx] = kRejected;
+        return;
+      }
+      all_decided &= x != kUndecided;
+    }
+  }
+  if (all_decided) status[idx] = kAccepted;
+  else atomicAdd(&undecided[e], 1u);
+}
+
+// used[e][v] for both ends of every accepted edge; flags for the two prefix
+// sums: accepted edges by rank, unused programs by id.
+__global__ void pat_flags(uint64_t n, uint64_t m, const uint32_t *order, const int32_t *nb,
+                          const uint8_t *status, uint8_t *used) {
+  const uint64_t idx = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (idx >= m) return;
+  if (status[idx] == kAccepted) {
+    const uint64_t e = idx / n;
+    used[idx] = 1;
+    used[e * n + static_cast<uint32_t>(nb[idx])] = 1;
+  }
+}
+
+__global__ void pat_count(uint64_t n, uint64_t m, const uint32_t *order, const uint8_t *status,
+                          const uint8_t *used, uint32_t *acc_by_rank, uint32_t *unused_by_id) {
+  const uint64_t idx = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (idx >= m) return;
+  const uint64_t e = idx / n;
+  acc_by_rank[idx] = status[e * n + order[idx]] == kAccepted;
+  unused_by_id[idx] = used[idx] == 0;
+}
+
+// The pairing: accepted edges in rank order (pos from the first scan), then
+// the unused programs in id order (pos from the second).  num_indices[e] =
+// the number of accepted edges.
+__global__ void pat_write(uint64_t n, uint64_t m, const uint32_t *order, const int32_t *nb,
+                          const uint8_t *status, const uint8_t *used, const uint32_t *acc_pos,
+                          const uint32_t *unused_pos, uint32_t *out, uint64_t *num_indices) {
+  const uint64_t idx = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (idx >= m) return;
+  const uint64_t e = idx / n, t = idx - e * n, base = e * n;
+  const uint64_t num = acc_pos[base + n - 1] +
+                       (status[base + order[base + n - 1]] == kAccepted ? 1 : 0);
+  const uint32_t i = order[idx];
+  if (status[base + i] == kAccepted) {
+    const uint32_t p = acc_pos[idx];
+    out[base + 2 * p] = i;
+    out[base + 2 * p + 1] = static_cast<uint32_t>(nb[base + i]);
+  }
+  if (used[idx] == 0) out[base + 2 * num + unused_pos[idx]] = static_cast<uint32_t>(t);
+  if (t == 0) num_indices[e] = num;
+}
+
 }  // namespace
+
+// Scratch of launch_pattern: the shuffle's own scratch, then order, rank,
+// nb, cnt, start, len, bucket, two scan arrays (uint32 each), status and
+// used (bytes), and one undecided counter per epoch.
+size_t pattern_scratch_bytes(uint64_t n, uint32_t n_epochs) {
+  const uint64_t m = n * n_epochs;
+  return shuffle_scratch_bytes(n, n_epochs) + 9 * m * sizeof(uint32_t) + 2 * m +
+         size_t(n_epochs) * sizeof(uint32_t) + 64;
+}
+
+int launch_pattern(uint64_t s0, uint64_t first_epoch, uint32_t E, uint64_t n,
+                   const uint32_t *offs, const uint32_t *tgts, uint32_t *out,
+                   uint64_t *num_indices, void *scratch, uint32_t *h_undecided,
+                   cudaStream_t stream) {
+  if (n == 0 || E == 0) return CUBFF_OK;
+  const uint64_t m = n * E;
+  uint8_t *p = static_cast<uint8_t *>(scratch);
+  void *fy = p;
+  p += shuffle_scratch_bytes(n, E);
+  auto take32 = [&]() {
+    uint32_t *a = reinterpret_cast<uint32_t *>(p);
+    p += m * sizeof(uint32_t);
+    return a;
+  };
+  uint32_t *order = take32(), *rank = take32();
+  int32_t *nb = reinterpret_cast<int32_t *>(take32());
+  uint32_t *cnt = take32(), *start = take32(), *len = take32(), *bucket = take32();
+  uint32_t *acc = take32(), *unused = take32();
+  uint8_t *status = p;
+  p += m;
+  uint8_t *used = p;
+  p += m;
+  p = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(p) + 15) & ~uintptr_t(15));
+  uint32_t *undecided = reinterpret_cast<uint32_t *>(p);
+  const unsigned blocks = blocks_for(m, 256);
+
+  CUBFF_TRY(launch_shuffle(s0, first_epoch, E, n, order, fy, stream));
+  CUBFF_TRY(launch_inverse(order, E, n, rank, stream));
+  CUBFF_CUDA_TRY(cudaMemsetAsync(cnt, 0, m * sizeof(uint32_t), stream));
+  CUBFF_CUDA_TRY(cudaMemsetAsync(used, 0, m, stream));
+  pat_propose<<<blocks, 256, 0, stream>>>(s0, first_epoch, n, m, offs, tgts, nb, cnt, status);
+  // In-degree counts -> lists: len keeps the counts, start their prefix sums.
+  CUBFF_CUDA_TRY(cudaMemcpyAsync(len, cnt, m * sizeof(uint32_t), cudaMemcpyDeviceToDevice, stream));
+  fy_scan<<<E, 1024, 0, stream>>>(n, cnt, start);  // (also zeroes cnt)
+  pat_fill<<<blocks, 256, 0, stream>>>(n, m, nb, cnt, start, bucket);
+  // Rounds until every edge is decided (checked every 8 rounds).
+  for (int checks = 0;; checks++) {
+    CUBFF_CUDA_TRY(cudaMemsetAsync(undecided, 0, E * sizeof(uint32_t), stream));
+    for (int r = 0; r < 8; r++) {
+      if (r == 7) CUBFF_CUDA_TRY(cudaMemsetAsync(undecided, 0, E * sizeof(uint32_t), stream));
+      pat_round<<<blocks, 256, 0, stream>>>(n, m, nb, rank, start, len, bucket, status, undecided);
+    }
+    CUBFF_CUDA_TRY(cudaMemcpyAsync(h_undecided, undecided, E * sizeof(uint32_t),
+                                   cudaMemcpyDeviceToHost, stream));
+    CUBFF_CUDA_TRY(cudaStreamSynchronize(stream));
+    uint64_t left = 0;
+    for (uint32_t e = 0; e < E; e++) left += h_undecided[e];
+    if (left == 0) break;
+    if (checks > static_cast<int>(n)) return set_error(CUBFF_EDEVICE, "pattern pairing did not converge");
+  }
+  pat_flags<<<blocks, 256, 0, stream>>>(n, m, order, nb, status, used);
+  pat_count<<<blocks, 256, 0, stream>>>(n, m, order, status, used, acc, unused);
+  // Exclusive prefix sums per epoch (in place: fy_scan reads cnt, writes start, zeroes cnt).
+  fy_scan<<<E, 1024, 0, stream>>>(n, acc, start);
+  fy_scan<<<E, 1024, 0, stream>>>(n, unused, len);
+  pat_write<<<blocks, 256, 0, stream>>>(n, m, order, nb, status, used, start, len, out, num_indices);
+  CUBFF_CUDA_TRY(cudaGetLastError());
+  return CUBFF_OK;
+}
 
 // Six uint32 arrays of n * n_epochs entries; SIZE_MAX when that does not fit
 // in size_t (so no scratch size can pass a check against it).

@@ -89,9 +89,14 @@ constexpr int kCountSlots = kPipeCountSlots;  // per-epoch counter slots (spread
 //
 // Launch-shape knobs (PipeTuning, chosen by the host):
 //  * steps_per_visit: interpreter steps a running lane takes per iteration of
-//    its warp, the same for every lane (an iteration lasts as long as its
-//    busiest lane, so a lane given more steps holds its warp-mates, and the
-//    pairs they would finish and notify, for its extra steps);
+//    its warp after its first (an iteration lasts as long as its busiest
+//    lane, so a lane given more steps holds its warp-mates, and the pairs
+//    they would finish and notify, for its extra steps);
+//  * first_visit_steps: the steps of a pair's first visit.  Lanes that claim
+//    together stage and start together, and most pairs end within a few
+//    steps; the first visit's budget bounds how long one heavy pair among
+//    them holds the others (whose consumers wait on them) before they can
+//    write back;
 //  * claim_min: a warp with running lanes claims new slots only once this
 //    many of its lanes are idle (an idle warp claims at once), so a slot held
 //    by a busy warp is polled only between its long iterations;
@@ -304,7 +309,8 @@ __device__ __forceinline__ bool iterate(const PipeCtx &b, const PipeQueue &q, La
     // 5. A few interpreter steps; on the end, write back and notify.
     progressed = true;
     bool fin = !ln.evaluated;
-    for (uint32_t r = 0; r < b.tune.steps_per_visit && !fin; r++) fin = m.step(t, stk, np, optab);
+    const uint32_t steps = ln.visits ? b.tune.steps_per_visit : b.tune.first_visit_steps;
+    for (uint32_t r = 0; r < steps && !fin; r++) fin = m.step(t, stk, np, optab);
     ln.visits++;
     if (fin) {
       const PipeSoup &sp = b.soups[ln.si];
@@ -487,18 +493,20 @@ cubff_tuning default_shape() {
   static const cubff_tuning t = {env_u32("CUBFF_LANES_PER_PAIR64", 32, 1, 64),
                                  env_u32("CUBFF_STEPS_PER_VISIT", 64, 1, 4096),
                                  env_u32("CUBFF_CLAIM_MIN", 20, 1, 32),
-                                 env_u32("CUBFF_LONG_VISITS", 1, 0, 1u << 20)};
+                                 env_u32("CUBFF_LONG_VISITS", 1, 0, 1u << 20),
+                                 env_u32("CUBFF_FIRST_VISIT_STEPS", 64, 1, 4096)};
   return t;
 }
 
 bool valid_shape(const cubff_tuning &t) {
   return t.lanes_per_pair64 >= 1 && t.lanes_per_pair64 <= 64 && t.steps_per_visit >= 1 &&
-         t.steps_per_visit <= 4096 && t.claim_min >= 1 && t.claim_min <= 32;
+         t.steps_per_visit <= 4096 && t.claim_min >= 1 && t.claim_min <= 32 &&
+         t.first_visit_steps >= 1 && t.first_visit_steps <= 4096;
 }
 
 PipeTuning pipe_tuning(const cubff_tuning &t) {
   return PipeTuning{t.steps_per_visit, t.claim_min,
-                    t.long_visits ? t.long_visits : 0xffffffffu};
+                    t.long_visits ? t.long_visits : 0xffffffffu, t.first_visit_steps};
 }
 
 int launch_pipeline(const PipeBatch &b, uint64_t total_pairs, uint32_t lanes_per_pair64,

@@ -120,11 +120,15 @@ int cubff_shuffle_indices(uint64_t params_seed, uint64_t first_epoch,
  * time does.  Chosen per launch group by the engine's tuner
  * (cubff_engine_tune), or set by hand. */
 typedef struct {
-  uint32_t lanes_per_pair64; /* lanes in flight per 64 pairs of an epoch (grid size)    */
-  uint32_t steps_per_visit;  /* interpreter steps a lane takes per iteration of its warp */
-  uint32_t claim_min;        /* idle lanes a busy warp needs before it claims new pairs   */
-  uint32_t long_visits;      /* a pair running longer than this many visits keeps its
-                                warp from claiming (0 = never)                            */
+  uint32_t lanes_per_pair64;  /* lanes in flight per 64 pairs of an epoch (grid size)    */
+  uint32_t steps_per_visit;   /* interpreter steps a lane takes per iteration of its warp
+                                 after its first                                        */
+  uint32_t claim_min;         /* idle lanes a busy warp needs before it claims new pairs  */
+  uint32_t long_visits;       /* a pair running longer than this many visits keeps its
+                                 warp from claiming (0 = never)                           */
+  uint32_t first_visit_steps; /* steps of a pair's first visit (most pairs end in it; a
+                                 small budget keeps one heavy pair from holding the
+                                 warp-mates that staged with it)                          */
 } cubff_tuning;
 
 /* The default launch shape (what a launch uses without a tuned one). */
@@ -272,7 +276,7 @@ uint64_t cubff_soup_footprint_bytes(const cubff_soup_params *params);
  *
  * cubff_engine_tune runs trial_epochs epochs of copies of the given soups
  * (their current bytes and epoch; the soups themselves are not advanced)
- * under candidate shapes, by coordinate descent over the four knobs from the
+ * under candidate shapes, by coordinate descent over the five knobs from the
  * default, checks that every candidate gives the same op counts, and caches
  * the fastest shape for each launch group the soups form.  chosen (nullable,
  * n_soups entries) receives the shape that now applies to each soup.
