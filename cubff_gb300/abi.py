@@ -32,7 +32,7 @@ class SoupParams(ctypes.Structure):
 class Tuning(ctypes.Structure):
     """cubff_tuning: the launch shape of a pipelined launch."""
     _fields_ = [("lanes_per_pair64", u32), ("steps_per_visit", u32), ("claim_min", u32),
-                ("long_visits", u32), ("first_visit_steps", u32)]
+                ("long_visits", u32), ("first_visit_steps", u32), ("long_lanes", u32)]
 
     def as_dict(self):
         return {f: int(getattr(self, f)) for f, _ in self._fields_}
@@ -90,6 +90,7 @@ SIGNATURES = {
     "cubff_server_fetch": (ci, [vp, u64, vp, vp]),
     "cubff_server_stats": (ci, [vp, vp, vp, vp, vp]),
     "cubff_eval_pair": (ci, [ci, vp, vp, vp]),
+    "cubff_soup_histogram": (ci, [vp, vp]),
     "cubff_eval_selfrep": (ci, [ci, vp, u64, vp]),
 }
 
@@ -220,6 +221,12 @@ class Soup:
         if want_shuffle:
             return ops, raw, shuf, ni
         return ops, raw
+
+    def histogram(self) -> np.ndarray:
+        """The soup's 256 byte counts, counted on the device."""
+        out = np.zeros(256, dtype=np.uint64)
+        check(lib().cubff_soup_histogram(self.h, _p(out)))
+        return out
 
     def selfrep(self, epoch: int) -> np.ndarray:
         out = np.zeros(self.num_programs, dtype=np.uint64)

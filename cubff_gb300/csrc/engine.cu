@@ -111,6 +111,8 @@ void cubff_soup::release() {
   d_inv = d_readycnt = nullptr;
   if (d_mutmask) cudaFree(d_mutmask);
   d_mutmask = nullptr;
+  if (d_hist) cudaFree(d_hist);
+  d_hist = nullptr;
   d_soup = nullptr;
   d_perm = nullptr;
   d_num_indices = nullptr;
@@ -324,7 +326,7 @@ uint64_t cubff_soup_footprint_bytes(const cubff_soup_params *params) {
   bytes += batch * P * sizeof(uint4);                             // mutation masks
   bytes += batch * n * sizeof(uint32_t);                          // inverse shuffles
   bytes += batch * P * sizeof(uint32_t);                          // ready counters
-  bytes += batch * P * sizeof(uint32_t);                          // ready-queue share
+  bytes += 2 * batch * P * sizeof(uint32_t);                      // ready and long queue share
   return bytes;
 }
 
@@ -447,6 +449,18 @@ int cubff_soup_selfrep(cubff_soup *soup, uint64_t epoch, uint64_t *result) {
   cudaFree(d_res);
   if (err != cudaSuccess) return set_error(CUBFF_EDEVICE, "soup_selfrep: %s", cudaGetErrorString(err));
   return st;
+}
+
+int cubff_soup_histogram(cubff_soup *soup, uint64_t *counts) {
+  if (!soup || !counts) return set_error(CUBFF_EINVAL, "soup_histogram: null argument");
+  CUBFF_CUDA_TRY(cudaSetDevice(soup->eng->device));
+  cudaStream_t st = soup->eng->stream;
+  if (!soup->d_hist) CUBFF_CUDA_TRY(cudaMalloc(&soup->d_hist, 256 * sizeof(unsigned long long)));
+  CUBFF_TRY(launch_histogram(soup->d_soup, soup->p.num_programs * kTape, soup->d_hist, st));
+  CUBFF_CUDA_TRY(cudaMemcpyAsync(counts, soup->d_hist, 256 * sizeof(unsigned long long),
+                                 cudaMemcpyDeviceToHost, st));
+  CUBFF_CUDA_TRY(cudaStreamSynchronize(st));
+  return CUBFF_OK;
 }
 
 int cubff_eval_pair(int lang, uint8_t *tape, uint64_t *ops, uint64_t *raw) {

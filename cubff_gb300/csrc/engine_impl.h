@@ -67,6 +67,7 @@ struct cubff_soup {
   uint4 *d_mutmask = nullptr;      // [batch][num_programs / 2] mutation masks
 
   bool dirty = false;              // a launch gave up: d_readycnt may be nonzero
+  unsigned long long *d_hist = nullptr;  // [256] byte counts (cubff_soup_histogram)
 
   // Per-epoch op / raw-step counters: kPipeCountSlots (ops, raw) pairs for
   // each of kCounterChunk epochs, reduced on the host.

@@ -8,6 +8,7 @@
 // the interpreter's data-dependent byte accesses never bank-conflict.  The
 // op count is reduced per warp (redux) and added with one atomic per warp, as
 // IncreaseInsnCount does (common_language.h:56-63).
+#include <algorithm>
 #include "internal.h"
 #include "epoch_body.cuh"
 
@@ -170,6 +171,38 @@ int launch_init(uint64_t key, uint64_t n, uint8_t *soup, int zero_init,
   const uint64_t chunks = count * 4;
   const unsigned grid = static_cast<unsigned>((chunks + 255) / 256);
   init_kernel<<<grid, 256, 0, stream>>>(soup, n, key, zero_init, count);
+  CUBFF_CUDA_TRY(cudaGetLastError());
+  return CUBFF_OK;
+}
+
+// Byte histogram of a soup (the statistics of common_language.h:519-533):
+// per-block counters in shared memory, added into 256 global counters.
+__global__ void histogram_kernel(const uint32_t *words, uint64_t n_words,
+                                 unsigned long long *counts) {
+  __shared__ uint32_t h[256];
+  for (uint32_t c = threadIdx.x; c < 256; c += blockDim.x) h[c] = 0;
+  __syncthreads();
+  for (uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n_words;
+       i += uint64_t(gridDim.x) * blockDim.x) {
+    const uint32_t w = words[i];
+    atomicAdd(&h[w & 0xFF], 1u);
+    atomicAdd(&h[(w >> 8) & 0xFF], 1u);
+    atomicAdd(&h[(w >> 16) & 0xFF], 1u);
+    atomicAdd(&h[w >> 24], 1u);
+  }
+  __syncthreads();
+  for (uint32_t c = threadIdx.x; c < 256; c += blockDim.x)
+    if (h[c]) atomicAdd(&counts[c], static_cast<unsigned long long>(h[c]));
+}
+
+int launch_histogram(const uint8_t *soup, uint64_t n_bytes, unsigned long long *counts,
+                     cudaStream_t stream) {
+  CUBFF_CUDA_TRY(cudaMemsetAsync(counts, 0, 256 * sizeof(unsigned long long), stream));
+  const uint64_t words = n_bytes / 4;  // soups are num_programs * 64 bytes
+  if (words == 0) return CUBFF_OK;
+  const unsigned blocks = static_cast<unsigned>(std::min<uint64_t>((words + 255) / 256, 1216));
+  histogram_kernel<<<blocks, 256, 0, stream>>>(reinterpret_cast<const uint32_t *>(soup), words,
+                                               counts);
   CUBFF_CUDA_TRY(cudaGetLastError());
   return CUBFF_OK;
 }

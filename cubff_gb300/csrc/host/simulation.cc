@@ -13,6 +13,8 @@
 #include <cstring>
 #include <memory>
 #include <mutex>
+#include <string>
+#include <thread>
 
 #include "cubff_gb300.h"
 #include "cubff_gb300_sim.h"
@@ -134,16 +136,16 @@ class Simulation : public LanguageInterface {
   int lang_;
 };
 
-// Callback statistics of common_language.h:504-561.
-void fill_stats(int lang, SimulationState &st, size_t num_programs, size_t insn, size_t num_runs) {
+// Callback statistics of common_language.h:504-561; counts = the soup's byte
+// histogram (counted on the device).
+void fill_stats(int lang, SimulationState &st, size_t num_programs, size_t insn, size_t num_runs,
+                const uint64_t *counts) {
   size_t bsize = 0;
   static bool warned = false;
   if (!BrotliSize(st.soup.data(), st.soup.size(), &bsize) && !warned) {
     fprintf(stderr, "cubff: libbrotlienc not found; brotli_size is reported as 0\n");
     warned = true;
   }
-  size_t counts[256] = {};
-  for (uint8_t c : st.soup) counts[c]++;
   std::vector<uint8_t> sorted(256);
   double h0 = 0;
   for (size_t i = 0; i < 256; i++) {
@@ -245,49 +247,88 @@ void Simulation::RunSimulation(const SimulationParams &params,
   const auto sim_start = clock::now();
   auto start = sim_start;
   const uint64_t ci = params.callback_interval;
-  std::vector<uint64_t> ops, ni;
-  while (true) {
+
+  // One segment of the loop: the epochs up to and including the next
+  // callback epoch (e % callback_interval == 0).
+  struct Segment {
+    uint64_t cb_epoch = 0, k = 0;
+    std::vector<uint64_t> ops, ni;
+    std::vector<uint32_t> shuffle;
+    int status = CUBFF_OK;
+    std::string error;
+  };
+  auto run_segment = [&](Segment &g) {
     uint64_t e0 = 0, ri = 0;
-    check(cubff_soup_get_epoch(soup.h, &e0, &ri));
-    const uint64_t cb_epoch = e0 + (ci - e0 % ci) % ci;  // next epoch with e % ci == 0
-    const uint64_t k = cb_epoch - e0 + 1;
-    ops.assign(k, 0);
-    ni.assign(k, 0);
-    check(cubff_soup_run(soup.h, k, ops.data(), nullptr, state.shuffle_idx.data(), ni.data()));
+    g.status = cubff_soup_get_epoch(soup.h, &e0, &ri);
+    if (g.status == CUBFF_OK) {
+      g.cb_epoch = e0 + (ci - e0 % ci) % ci;
+      g.k = g.cb_epoch - e0 + 1;
+      g.ops.assign(g.k, 0);
+      g.ni.assign(g.k, 0);
+      g.shuffle.resize(num_programs);
+      g.status = cubff_soup_run(soup.h, g.k, g.ops.data(), nullptr, g.shuffle.data(), g.ni.data());
+    }
+    if (g.status != CUBFF_OK) g.error = cubff_last_error();
+  };
+  // While the host computes a callback's statistics (brotli) and runs the
+  // callback, the next segment already runs on the device, from a worker
+  // thread.  The callback sees the soup as it was at its epoch (copied to
+  // the host before the next segment starts); if it stops the run, the extra
+  // segment's work is dropped with the soup.
+  Segment cur, next;
+  struct Joiner {  // declared after the segments, so it joins before they go
+    std::thread t;
+    ~Joiner() {
+      if (t.joinable()) t.join();
+    }
+  } ahead;
+  run_segment(cur);
+  while (true) {
+    if (cur.status != CUBFF_OK) throw Error(cur.status, cur.error);
     const auto stop = clock::now();
     size_t insn = 0, num_runs = 0;
-    for (uint64_t q = 0; q < k; q++) {
-      insn += ops[q];
-      num_runs += ni[q];
+    for (uint64_t q = 0; q < cur.k; q++) {
+      insn += cur.ops[q];
+      num_runs += cur.ni[q];
     }
     total_ops += insn;
+    uint64_t e_now = 0, ri = 0;
+    check(cubff_soup_get_epoch(soup.h, &e_now, &ri));
     check(cubff_soup_read(soup.h, state.soup.data(), 0, state.soup.size()));
+    uint64_t counts[256];
+    check(cubff_soup_histogram(soup.h, counts));
+    state.shuffle_idx.assign(cur.shuffle.begin(), cur.shuffle.end());
+    if (params.eval_selfrep) {  // :563-569, on the soup of this callback's epoch
+      std::vector<uint64_t> rep(num_programs);
+      check(cubff_soup_selfrep(soup.h, cur.cb_epoch, rep.data()));
+      for (size_t i = 0; i < num_programs; i++) state.replication_per_prog[i] = rep[i];
+    }
+    next = Segment();
+    ahead.t = std::thread([&] { run_segment(next); });
     const float elapsed = std::chrono::duration_cast<std::chrono::microseconds>(stop - start).count() * 1e-6;
     const float sim_elapsed =
         std::chrono::duration_cast<std::chrono::microseconds>(stop - sim_start).count() * 1e-6;
-    fill_stats(lang_, state, num_programs, insn, num_runs);
+    fill_stats(lang_, state, num_programs, insn, num_runs, counts);
     state.elapsed_s = sim_elapsed;
     state.total_ops = total_ops;
     state.mops_s = elapsed > 0 ? insn * 1.0 / elapsed * 1e-6 : 0.0f;
-    state.epoch = cb_epoch + 1;
-    if (params.eval_selfrep) {  // :563-569
-      std::vector<uint64_t> rep(num_programs);
-      check(cubff_soup_selfrep(soup.h, cb_epoch, rep.data()));
-      for (size_t i = 0; i < num_programs; i++) state.replication_per_prog[i] = rep[i];
-    }
-    if (params.save_to && params.save_interval && cb_epoch % params.save_interval == 0) {
+    state.epoch = cur.cb_epoch + 1;
+    if (params.save_to && params.save_interval && cur.cb_epoch % params.save_interval == 0) {
       char path[4096];  // :570-581
       snprintf(path, sizeof(path), "%s/%010llu.dat", params.save_to->c_str(),
-               static_cast<unsigned long long>(cb_epoch));
+               static_cast<unsigned long long>(cur.cb_epoch));
       FILE *f = fopen(path, "wb");
       if (!f) throw Error(CUBFF_EINVAL, std::string("Could not open ") + path);
-      const uint64_t hdr[3] = {ri, num_programs, cb_epoch + 1};
+      const uint64_t hdr[3] = {ri, num_programs, cur.cb_epoch + 1};
       fwrite(hdr, sizeof(uint64_t), 3, f);
       fwrite(state.soup.data(), 1, state.soup.size(), f);
       fclose(f);
     }
-    if (callback(state)) break;
-    start = clock::now();
+    const bool done = callback(state);
+    ahead.t.join();
+    if (done) break;
+    start = stop;
+    cur = std::move(next);
   }
 }
 

@@ -27,13 +27,13 @@ def _oracle(lang, n, seed, epochs):
 
 
 SHAPES = [dict(lanes_per_pair64=16, steps_per_visit=16, claim_min=8, long_visits=0,
-               first_visit_steps=16),
+               first_visit_steps=16, long_lanes=0),
           dict(lanes_per_pair64=64, steps_per_visit=256, claim_min=32, long_visits=8,
-               first_visit_steps=4),
+               first_visit_steps=4, long_lanes=8),
           dict(lanes_per_pair64=24, steps_per_visit=1, claim_min=1, long_visits=1,
-               first_visit_steps=1),
+               first_visit_steps=1, long_lanes=1),
           dict(lanes_per_pair64=48, steps_per_visit=128, claim_min=26, long_visits=2,
-               first_visit_steps=8)]
+               first_visit_steps=8, long_lanes=32)]
 
 
 @pytest.mark.parametrize("shape", SHAPES)
@@ -41,14 +41,16 @@ SHAPES = [dict(lanes_per_pair64=16, steps_per_visit=16, claim_min=8, long_visits
                                     ("bff_selfmove", 1024)])
 def test_results_are_identical_under_every_shape(lang, n, shape):
     eng = abi.Engine(0)
-    eng.set_tuning(lang, n, 1, **shape)
-    assert eng.get_tuning(lang, n, 1) == shape
-    s = abi.Soup(eng, lang, n, 41)
-    ops, _ = s.run(24)
-    want_ops, want_soup = _oracle(lang, n, 41, 24)
-    assert [int(x) for x in ops] == want_ops
-    assert np.array_equal(s.read(), want_soup)
-    eng.close()
+    try:
+        eng.set_tuning(lang, n, 1, **shape)
+        assert eng.get_tuning(lang, n, 1) == shape
+        s = abi.Soup(eng, lang, n, 41)
+        ops, _ = s.run(24)
+        want_ops, want_soup = _oracle(lang, n, 41, 24)
+        assert [int(x) for x in ops] == want_ops
+        assert np.array_equal(s.read(), want_soup)
+    finally:
+        eng.close()
 
 
 @pytest.mark.parametrize("shape", SHAPES[:2])
