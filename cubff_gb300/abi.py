@@ -32,7 +32,7 @@ class SoupParams(ctypes.Structure):
 class Tuning(ctypes.Structure):
     """cubff_tuning: the launch shape of a pipelined launch."""
     _fields_ = [("lanes_per_pair64", u32), ("steps_per_visit", u32), ("claim_min", u32),
-                ("long_visits", u32), ("first_visit_steps", u32), ("long_lanes", u32)]
+                ("long_visits", u32), ("first_visit_steps", u32)]
 
     def as_dict(self):
         return {f: int(getattr(self, f)) for f, _ in self._fields_}

@@ -48,8 +48,8 @@ int cubff_engine::reserve_pipe(size_t groups, size_t entries) {
     if (h_ctl) cudaFreeHost(h_ctl);
     d_ctl = h_ctl = nullptr;
     ctl_groups = 0;
-    CUBFF_CUDA_TRY(cudaMalloc(&d_ctl, groups * kPipeCtlWords * sizeof(uint32_t)));
-    CUBFF_CUDA_TRY(cudaMallocHost(&h_ctl, groups * kPipeCtlWords * sizeof(uint32_t)));
+    CUBFF_CUDA_TRY(cudaMalloc(&d_ctl, groups * 4 * sizeof(uint32_t)));
+    CUBFF_CUDA_TRY(cudaMallocHost(&h_ctl, groups * 4 * sizeof(uint32_t)));
     ctl_groups = groups;
   }
   if (entries > queue_cap) {
@@ -86,7 +86,6 @@ struct Group {
   std::vector<int> members;  // indices into the run's soups
   cudaStream_t st;
   size_t qoff;               // first entry of the group's ready queue in d_queue
-  size_t qlen = 0;           // its entries; the long queue follows (as many again)
   uint64_t programs = 0;     // summed over the members (the launch-shape key)
 };
 
@@ -105,7 +104,7 @@ static int read_counters(cubff_soup *const *soups, const std::vector<Group> &gro
                          std::vector<Progress> &pr, uint64_t *const *ops, uint64_t *const *raw,
                          const uint32_t *h_ctl, uint32_t *fault) {
   for (const Group &g : groups) {
-    *fault = std::max(*fault, h_ctl[kPipeCtlWords * (&g - groups.data()) + 2]);
+    *fault = std::max(*fault, h_ctl[4 * (&g - groups.data()) + 2]);
     for (int i : g.members) {
       const uint64_t rows = pr[i].done - pr[i].cbase;
       const unsigned long long *h = soups[i]->h_counters;
@@ -135,8 +134,8 @@ static int copy_counters(cubff_soup *const *soups, const std::vector<Group> &gro
                                        rows * kPipeCountSlots * 2 * sizeof(unsigned long long),
                                        cudaMemcpyDeviceToHost, g.st));
     }
-    CUBFF_CUDA_TRY(cudaMemcpyAsync(eng->h_ctl + kPipeCtlWords * gi, eng->d_ctl + kPipeCtlWords * gi,
-                                   kPipeCtlWords * sizeof(uint32_t), cudaMemcpyDeviceToHost, g.st));
+    CUBFF_CUDA_TRY(cudaMemcpyAsync(eng->h_ctl + 4 * gi, eng->d_ctl + 4 * gi, 4 * sizeof(uint32_t),
+                                   cudaMemcpyDeviceToHost, g.st));
   }
   return CUBFF_OK;
 }
@@ -163,11 +162,10 @@ int run_soups(cubff_engine *eng, cubff_soup *const *soups, int n_soups, uint64_t
   for (int i : order) {
     if (groups.empty() || groups.back().lang != soups[i]->p.lang ||
         groups.back().members.size() == size_t(kMaxPipeSoups))
-      groups.push_back(Group{soups[i]->p.lang, {}, nullptr, entries, 0, 0});
+      groups.push_back(Group{soups[i]->p.lang, {}, nullptr, entries, 0});
     groups.back().members.push_back(i);
     groups.back().programs += soups[i]->p.num_programs;
-    groups.back().qlen += size_t(soups[i]->batch) * (soups[i]->p.num_programs / 2);
-    entries += 2 * size_t(soups[i]->batch) * (soups[i]->p.num_programs / 2);
+    entries += size_t(soups[i]->batch) * (soups[i]->p.num_programs / 2);
   }
   const size_t G = groups.size();
   CUBFF_TRY(eng->reserve_pipe(G, entries));
@@ -188,7 +186,7 @@ int run_soups(cubff_engine *eng, cubff_soup *const *soups, int n_soups, uint64_t
       s->dirty = false;
     }
   }
-  CUBFF_CUDA_TRY(cudaMemsetAsync(eng->d_ctl, 0, G * kPipeCtlWords * sizeof(uint32_t), main));
+  CUBFF_CUDA_TRY(cudaMemsetAsync(eng->d_ctl, 0, G * 4 * sizeof(uint32_t), main));
   if (G > 1) {
     CUBFF_CUDA_TRY(cudaEventRecord(eng->events[0], main));
     for (size_t g = 0; g < G; g++) CUBFF_CUDA_TRY(cudaStreamWaitEvent(groups[g].st, eng->events[0], 0));
@@ -292,20 +290,17 @@ int run_soups(cubff_engine *eng, cubff_soup *const *soups, int n_soups, uint64_t
       any = true;
       PipeQueue &q = pb.queue;
       q.queue = eng->d_queue + g.qoff;
-      q.lqueue = eng->d_queue + g.qoff + g.qlen;
-      q.ctl = eng->d_ctl + kPipeCtlWords * gi;
+      q.ctl = eng->d_ctl + 4 * gi;
       q.total = static_cast<uint32_t>(tasks);
       q.initial = initial;
       q.first_soup = 0;
       q.n_soups = static_cast<uint32_t>(pb.n_soups);
       q.lang = g.lang;
-      pb.error = reinterpret_cast<int *>(eng->d_ctl + kPipeCtlWords * gi + 2);
+      pb.error = reinterpret_cast<int *>(eng->d_ctl + 4 * gi + 2);
       pb.wait_limit_ns = pipeline_wait_limit_ns();
       const cubff_tuning shape = eng->shape_for(g.lang, g.programs, static_cast<uint32_t>(g.members.size()));
       pb.tune = pipe_tuning(shape);
-      // Queue heads and tails, the finished-task count (the error flag stays).
-      CUBFF_CUDA_TRY(cudaMemsetAsync(q.ctl, 0, 2 * sizeof(uint32_t), g.st));
-      CUBFF_CUDA_TRY(cudaMemsetAsync(q.ctl + 4, 0, 3 * sizeof(uint32_t), g.st));
+      CUBFF_CUDA_TRY(cudaMemsetAsync(q.ctl, 0, 2 * sizeof(uint32_t), g.st));  // head, tail
       CUBFF_TRY(launch_pipeline(pb, pairs, shape.lanes_per_pair64, eng->device, g.st));
       for (int i : g.members) {
         cubff_soup *s = soups[i];

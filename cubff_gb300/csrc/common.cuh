@@ -62,16 +62,6 @@ __device__ __forceinline__ uint32_t lane_base(uint32_t tid) {
 // leave the thread's own 128 bytes: every interpreter keeps its positions in
 // 0..127 anyway, and the parity tests would show any position that relied on
 // the wrap.
-//
-// Accesses are volatile on the device: each get and set is one shared-memory
-// access, issued in program order.  The interpreters already keep what they
-// reuse in registers (the bytes under the heads, the prefetched next-command
-// entry), so this costs few extra loads.  The fully optimised build with
-// plain accesses gave wrong op counts for bff_selfmove in about one run in
-// four (never in the host-compiled interpreter, whatever the leftover
-// shared-memory contents); volatile accesses, any of the interpreter's step
-// functions kept out of line, or a lower optimisation level in either the
-// device compiler or the assembler each removed it.
 #ifdef CUBFF_HOST_INDEX_CHECK
 // Host-compiled analysis builds only: reports every position outside the
 // accessor's range before it is wrapped or clamped.
@@ -87,12 +77,11 @@ struct LaneBytes {
   uint32_t base;  // lane_base(tid)
   __host__ __device__ __forceinline__ uint32_t get(int p) const {
     CUBFF_CHECK_POS(0, p, kPair - 1);
-    return static_cast<volatile uint8_t *>(s)[base + ((static_cast<uint32_t>(p) & (kPair - 1)) << 7)];
+    return s[base + ((static_cast<uint32_t>(p) & (kPair - 1)) << 7)];
   }
   __host__ __device__ __forceinline__ void set(int p, uint32_t v) const {
     CUBFF_CHECK_POS(1, p, kPair - 1);
-    static_cast<volatile uint8_t *>(s)[base + ((static_cast<uint32_t>(p) & (kPair - 1)) << 7)] =
-        static_cast<uint8_t>(v);
+    s[base + ((static_cast<uint32_t>(p) & (kPair - 1)) << 7)] = static_cast<uint8_t>(v);
   }
 };
 
@@ -106,8 +95,7 @@ constexpr int kNpEntries = kPair + 1 + kNpSpare;
 constexpr int kNpBytes = kNpEntries * 128 * 2;
 
 // Entries are clamped to the last one (kNpEntries - 1) for the same reason:
-// the array never reaches past its thread's column; accesses are volatile as
-// above.
+// the array never reaches past its thread's column.
 struct LaneNp {
   uint16_t *s;    // nullptr: no array (the interpreter stays in its basic mode)
   uint32_t base;  // tid within the 128-thread block
@@ -117,11 +105,11 @@ struct LaneNp {
   }
   __host__ __device__ __forceinline__ uint32_t get(int p) const {
     CUBFF_CHECK_POS(2, p, kNpEntries - 1);
-    return static_cast<volatile uint16_t *>(s)[base + (clamp(p) << 7)];
+    return s[base + (clamp(p) << 7)];
   }
   __host__ __device__ __forceinline__ void set(int p, uint32_t v) const {
     CUBFF_CHECK_POS(3, p, kNpEntries - 1);
-    static_cast<volatile uint16_t *>(s)[base + (clamp(p) << 7)] = static_cast<uint16_t>(v);
+    s[base + (clamp(p) << 7)] = static_cast<uint16_t>(v);
   }
 };
 

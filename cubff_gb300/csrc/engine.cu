@@ -326,7 +326,7 @@ uint64_t cubff_soup_footprint_bytes(const cubff_soup_params *params) {
   bytes += batch * P * sizeof(uint4);                             // mutation masks
   bytes += batch * n * sizeof(uint32_t);                          // inverse shuffles
   bytes += batch * P * sizeof(uint32_t);                          // ready counters
-  bytes += 2 * batch * P * sizeof(uint32_t);                      // ready and long queue share
+  bytes += batch * P * sizeof(uint32_t);                          // ready-queue share
   return bytes;
 }
 

@@ -63,15 +63,11 @@ struct PipeSoup {
 
 struct PipeQueue {
   uint32_t *queue;              // ready tasks + 1; total - initial entries, zero, left zero
-  uint32_t *lqueue;             // long tasks + 1 (handed to long warps); total entries,
-                                // zero, left zero
-  uint32_t *ctl;                // kPipeCtlWords words, zeroed: [0] head, [1] tail,
-                                // [2] error, [4] long head, [5] long tail, [6] tasks done
+  uint32_t *ctl;                // [0] head, [1] tail; zeroed
   uint32_t total, initial;      // tasks of this language; those of the first epoch
   uint32_t first_soup, n_soups;
   int lang;
 };
-constexpr int kPipeCtlWords = 8;
 
 // Everything a pipelined launch needs, passed by value as the kernel's
 // (grid-constant) parameter, so that a launch needs no host-to-device copy
@@ -85,14 +81,11 @@ struct PipeTuning {
   uint32_t long_visits;      // visits after which a pair counts as long: its warp stops
                              // claiming, so the pair runs without new warp-mates
   uint32_t first_visit_steps;  // steps of a pair's first visit
-  uint32_t long_lanes;       // > 0: the last warp of every block runs long pairs on this
-                             // many lanes; other warps hand a pair still running after its
-                             // first visit to them (it restarts from its inputs there)
 };
 // The default launch shape (cubff_tuning: lanes in flight per 64 pairs, then
 // the PipeTuning knobs; long_visits 0 = never), each knob overridable by the
 // environment (CUBFF_LANES_PER_PAIR64, CUBFF_STEPS_PER_VISIT, CUBFF_CLAIM_MIN,
-// CUBFF_LONG_VISITS, CUBFF_FIRST_VISIT_STEPS, CUBFF_LONG_LANES), read once.
+// CUBFF_LONG_VISITS, CUBFF_FIRST_VISIT_STEPS), read once.
 cubff_tuning default_shape();
 // The kernel's view of a shape; false when a knob is out of range.
 bool valid_shape(const cubff_tuning &t);

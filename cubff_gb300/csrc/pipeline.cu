@@ -100,17 +100,6 @@ constexpr int kCountSlots = kPipeCountSlots;  // per-epoch counter slots (spread
 //  * claim_min: a warp with running lanes claims new slots only once this
 //    many of its lanes are idle (an idle warp claims at once), so a slot held
 //    by a busy warp is polled only between its long iterations;
-//  * long_lanes (> 0): the last warp of every block is a long warp.  It
-//    serves only the long queue, on its first long_lanes lanes (the others
-//    stay out).  Any other warp runs a pair for its first visit only: a pair
-//    still running then is handed to the long queue and its lane freed.  The
-//    pair has written nothing and notified no one, so a long lane restarts it
-//    from the same inputs (gather, mutation mask) and gets the same result.
-//    Ordinary warps then hold only pairs that end within one visit, so the
-//    many short pairs each epoch waits on are not held by a heavy warp-mate,
-//    and long pairs step with few warp-mates.  Long lanes wait for the long
-//    queue until every task of the launch is done (a count kept in ctl[6]);
-//    their wait limit restarts whenever that count moves;
 //  * long_visits: a pair still running after this many visits is long.  A
 //    warp holding a long pair claims nothing new: its other lanes drain, and
 //    the long pair, which the next epochs' pairs wait on, steps without
@@ -174,7 +163,7 @@ __device__ __forceinline__ bool iterate(const PipeCtx &b, const PipeQueue &q, La
                                         LaneMachine<L> &m, const LaneBytes t, const LaneBytes stk,
                                         const LaneNp np, const uint8_t *__restrict__ optab,
                                         const uint8_t *__restrict__ cmdflag, uint32_t lane,
-                                        uint32_t slot_ctr, bool long_warp) {
+                                        uint32_t slot_ctr) {
   constexpr bool kBffFam = (L <= kBffSelfmove);
   const uint32_t lt_mask = (1u << lane) - 1;
   const int s_lo = static_cast<int>(q.first_soup), s_hi = static_cast<int>(q.first_soup + q.n_soups);
@@ -183,24 +172,7 @@ __device__ __forceinline__ bool iterate(const PipeCtx &b, const PipeQueue &q, La
   const uint32_t idle = __ballot_sync(0xffffffffu, ln.state == kIdle);
   const uint32_t busy = __ballot_sync(0xffffffffu, ln.state != kIdle && ln.state != kExhausted);
   const uint32_t lng = __ballot_sync(0xffffffffu, ln.state == kRun && ln.visits >= b.tune.long_visits);
-  if (long_warp && idle) {
-    // Long warps claim from the long queue only; slots past its capacity
-    // never fill (each task is handed over at most once) and just wait for
-    // the launch to finish.
-    const int leader = __ffs(idle) - 1;
-    uint32_t base = 0;
-    if (lane == static_cast<uint32_t>(leader)) base = atomicAdd(q.ctl + 4, __popc(idle));
-    base = __shfl_sync(0xffffffffu, base, leader);
-    if (ln.state == kIdle) {
-      ln.slot = base + __popc(idle & lt_mask);
-      ln.state = kSlot;
-      ln.qv = ln.slot < q.total ? ld_relaxed(q.lqueue + ln.slot) : 0;
-      ln.poll_gap = 1;
-      ln.poll_in = 0;
-      ln.t_wait = 0;
-      ln.c1 = 0;
-    }
-  } else if (!long_warp && idle && (busy == 0 || (lng == 0 && __popc(idle) >= b.tune.claim_min))) {
+  if (idle && (busy == 0 || (lng == 0 && __popc(idle) >= b.tune.claim_min))) {
     const int leader = __ffs(idle) - 1;
     uint32_t base = 0;
     if (lane == static_cast<uint32_t>(leader)) base = atomicAdd(q.ctl, __popc(idle));
@@ -213,10 +185,8 @@ __device__ __forceinline__ bool iterate(const PipeCtx &b, const PipeQueue &q, La
         ln.si = soup_of_slot(b.soups, s_lo, s_hi, ln.slot);
         const PipeSoup &sp = b.soups[ln.si];
         ln.task = sp.task_base + (ln.slot - sp.init_base);
-        ln.e = 0;
-        ln.k = ln.slot - sp.init_base;
         ln.state = kIndex;
-        ln.qp = *reinterpret_cast<const unsigned long long *>(sp.perm + 2 * uint64_t(ln.k));
+        ln.qp = *reinterpret_cast<const unsigned long long *>(sp.perm + 2 * uint64_t(ln.slot - sp.init_base));
       } else {
         ln.state = kSlot;
         ln.qv = ld_relaxed(q.queue + (ln.slot - q.initial));
@@ -227,7 +197,6 @@ __device__ __forceinline__ bool iterate(const PipeCtx &b, const PipeQueue &q, La
     }
   }
   bool progressed = false;
-  bool finished = false;  // a pair of this lane ended in this iteration
 
   if (ln.state == kSlot) {
     // 2. Waiting for the claimed slot's entry (polled in an earlier iteration).
@@ -239,8 +208,7 @@ __device__ __forceinline__ bool iterate(const PipeCtx &b, const PipeQueue &q, La
     } else if (ln.qv != 0) {
       ln.task = ln.qv - 1;
       // Consumed: leave the entry zero for the next launch.
-      if (long_warp) q.lqueue[ln.slot] = 0;
-      else q.queue[ln.slot - q.initial] = 0;
+      q.queue[ln.slot - q.initial] = 0;
       ln.si = soup_of_task(b.soups, s_lo, s_hi, ln.task);
       const PipeSoup &sp = b.soups[ln.si];
       const uint32_t rel = ln.task - sp.task_base;
@@ -251,24 +219,19 @@ __device__ __forceinline__ bool iterate(const PipeCtx &b, const PipeQueue &q, La
       ln.state = kIndex;
       progressed = true;
     } else if (ln.poll_in-- == 0) {
-      // Long lanes: the launch is over once every task is done; the wait
-      // limit counts from the last time that count moved.
-      const uint32_t done = long_warp ? ld_relaxed(q.ctl + 6) : 0;
-      if (ln.err || (long_warp && done >= q.total)) {
+      if (ln.err) {
         ln.state = kExhausted;
       } else {
         const uint64_t now = globaltimer_ns();
-        if (ln.t_wait == 0 || (long_warp && done != ln.c1)) {
+        if (ln.t_wait == 0) {
           ln.t_wait = now;
-          ln.c1 = done;
         } else if (now - ln.t_wait > b.wait_limit_ns) {
           atomicExch(b.error, 1);
           ln.state = kExhausted;
         }
       }
       if (ln.state == kSlot) {
-        if (long_warp) ln.qv = ln.slot < q.total ? ld_relaxed(q.lqueue + ln.slot) : 0;
-        else ln.qv = ld_relaxed(q.queue + (ln.slot - q.initial));
+        ln.qv = ld_relaxed(q.queue + (ln.slot - q.initial));
         ln.err = ld_relaxed(reinterpret_cast<const uint32_t *>(b.error));
         ln.poll_gap = ln.poll_gap < 16 ? ln.poll_gap * 2 : 16;
         ln.poll_in = ln.poll_gap;
@@ -278,6 +241,10 @@ __device__ __forceinline__ bool iterate(const PipeCtx &b, const PipeQueue &q, La
     // 3. Shuffle indices landed: order after the producers, issue the gather,
     //    the mutation mask and the next epoch's positions of both programs.
     const PipeSoup &sp = b.soups[ln.si];
+    if (ln.slot < q.initial) {
+      ln.e = 0;
+      ln.k = ln.slot - sp.init_base;
+    }
     ln.p1 = static_cast<uint32_t>(ln.qp);
     ln.p2 = static_cast<uint32_t>(ln.qp >> 32);
     fence_acq_rel_gpu();
@@ -345,16 +312,7 @@ __device__ __forceinline__ bool iterate(const PipeCtx &b, const PipeQueue &q, La
     const uint32_t steps = ln.visits ? b.tune.steps_per_visit : b.tune.first_visit_steps;
     for (uint32_t r = 0; r < steps && !fin; r++) fin = m.step(t, stk, np, optab);
     ln.visits++;
-    if (!fin && !long_warp && b.tune.long_lanes) {
-      // Hand the pair to the long warps (it restarts there from its inputs,
-      // which nothing has written yet).  Each task is handed over at most
-      // once, so the long queue's total entries suffice.
-      const uint32_t slot = atomicAdd(q.ctl + 5, 1u);
-      st_release_u32(q.lqueue + slot, ln.task + 1);
-      ln.state = kIdle;
-    }
     if (fin) {
-      finished = true;
       const PipeSoup &sp = b.soups[ln.si];
       if (ln.dirty || (ln.evaluated && m.mods() != 0)) {
         uint32_t w[32];
@@ -409,10 +367,6 @@ __device__ __forceinline__ bool iterate(const PipeCtx &b, const PipeQueue &q, La
                      next + (ln.j2 >> 1) + 1);
   }
   if (ln.state == kNotify) ln.state = kIdle;
-  if (b.tune.long_lanes) {
-    const uint32_t fm = __ballot_sync(0xffffffffu, finished);
-    if (fm && lane == static_cast<uint32_t>(__ffs(fm) - 1)) atomicAdd(q.ctl + 6, __popc(fm));
-  }
   return progressed;
 }
 
@@ -422,9 +376,9 @@ __device__ __forceinline__ void serve(const PipeCtx &b, const PipeQueue &q,
                                       const uint8_t *__restrict__ optab,
                                       const uint8_t *__restrict__ cmdflag, const LaneBytes t,
                                       const LaneBytes stk, const LaneNp np, uint32_t lane,
-                                      uint32_t slot_ctr, bool long_warp) {
+                                      uint32_t slot_ctr) {
   Lane ln;
-  ln.state = (long_warp && lane >= b.tune.long_lanes) ? kExhausted : kIdle;
+  ln.state = kIdle;
   ln.slot = ln.task = ln.e = ln.k = ln.p1 = ln.p2 = ln.qv = 0;
   ln.poll_gap = 1;
   ln.poll_in = ln.err = ln.j1 = ln.j2 = ln.c1 = ln.c2 = ln.visits = 0;
@@ -434,8 +388,7 @@ __device__ __forceinline__ void serve(const PipeCtx &b, const PipeQueue &q,
   ln.mm = make_uint4(0, 0, 0, 0);
   LaneMachine<L> m;
   while (true) {
-    const bool progressed =
-        iterate<L>(b, q, ln, m, t, stk, np, optab, cmdflag, lane, slot_ctr, long_warp);
+    const bool progressed = iterate<L>(b, q, ln, m, t, stk, np, optab, cmdflag, lane, slot_ctr);
     if (__all_sync(0xffffffffu, ln.state == kExhausted)) return;
     if (!__any_sync(0xffffffffu, progressed)) __nanosleep(200);
   }
@@ -486,8 +439,7 @@ __global__ void __launch_bounds__(kThreads, (L <= kBffSelfmove) ? 3 : 4)
   const LaneNp np{L <= kBffSelfmove ? npa : nullptr, tid};
   const PipeCtx b{soups, pb.error, pb.wait_limit_ns, pb.tune};
   const PipeQueue q = pb.queue;
-  const bool long_warp = b.tune.long_lanes != 0 && (tid >> 5) == kThreads / 32 - 1;
-  serve<L>(b, q, optab, cmdflag, t, stk, np, lane, warp % kCountSlots, long_warp);
+  serve<L>(b, q, optab, cmdflag, t, stk, np, lane, warp % kCountSlots);
 }
 
 template <int L>
@@ -542,21 +494,19 @@ cubff_tuning default_shape() {
                                  env_u32("CUBFF_STEPS_PER_VISIT", 64, 1, 4096),
                                  env_u32("CUBFF_CLAIM_MIN", 20, 1, 32),
                                  env_u32("CUBFF_LONG_VISITS", 1, 0, 1u << 20),
-                                 env_u32("CUBFF_FIRST_VISIT_STEPS", 64, 1, 4096),
-                                 env_u32("CUBFF_LONG_LANES", 0, 0, 32)};
+                                 env_u32("CUBFF_FIRST_VISIT_STEPS", 64, 1, 4096)};
   return t;
 }
 
 bool valid_shape(const cubff_tuning &t) {
   return t.lanes_per_pair64 >= 1 && t.lanes_per_pair64 <= 64 && t.steps_per_visit >= 1 &&
          t.steps_per_visit <= 4096 && t.claim_min >= 1 && t.claim_min <= 32 &&
-         t.first_visit_steps >= 1 && t.first_visit_steps <= 4096 && t.long_lanes <= 32;
+         t.first_visit_steps >= 1 && t.first_visit_steps <= 4096;
 }
 
 PipeTuning pipe_tuning(const cubff_tuning &t) {
   return PipeTuning{t.steps_per_visit, t.claim_min,
-                    t.long_visits ? t.long_visits : 0xffffffffu, t.first_visit_steps,
-                    t.long_lanes};
+                    t.long_visits ? t.long_visits : 0xffffffffu, t.first_visit_steps};
 }
 
 int launch_pipeline(const PipeBatch &b, uint64_t total_pairs, uint32_t lanes_per_pair64,
@@ -605,7 +555,7 @@ namespace {
 
 struct RunWs {
   uint4 *mutmask;
-  uint32_t *inv, *readycnt, *queue, *lqueue, *ctl;
+  uint32_t *inv, *readycnt, *queue, *ctl;
   unsigned long long *counters;
 };
 
@@ -622,8 +572,6 @@ RunWs run_ws(void *base, uint64_t n, uint32_t E) {
   w.readycnt = reinterpret_cast<uint32_t *>(p);
   p += align256(size_t(E) * P * sizeof(uint32_t));
   w.queue = reinterpret_cast<uint32_t *>(p);
-  p += align256(size_t(E) * P * sizeof(uint32_t));
-  w.lqueue = reinterpret_cast<uint32_t *>(p);
   p += align256(size_t(E) * P * sizeof(uint32_t));
   w.counters = reinterpret_cast<unsigned long long *>(p);
   p += align256(size_t(E) * kPipeCountSlots * 2 * sizeof(unsigned long long));
@@ -653,7 +601,7 @@ extern "C" size_t cubff_run_epochs_workspace_bytes(uint64_t num_programs, uint32
   const uint64_t P = num_programs / 2;
   return align256(size_t(n_epochs) * P * sizeof(uint4)) +
          align256(size_t(n_epochs) * num_programs * sizeof(uint32_t)) +
-         3 * align256(size_t(n_epochs) * P * sizeof(uint32_t)) +
+         2 * align256(size_t(n_epochs) * P * sizeof(uint32_t)) +
          align256(size_t(n_epochs) * kPipeCountSlots * 2 * sizeof(unsigned long long)) + 256;
 }
 
@@ -702,10 +650,9 @@ extern "C" int cubff_run_epochs_tuned(int lang, uint8_t *d_programs, const uint3
   RunWs w = run_ws(d_workspace, n, n_epochs);
   CUBFF_CUDA_TRY(cudaMemsetAsync(w.readycnt, 0, size_t(n_epochs) * P * sizeof(uint32_t), st));
   CUBFF_CUDA_TRY(cudaMemsetAsync(w.queue, 0, size_t(n_epochs) * P * sizeof(uint32_t), st));
-  CUBFF_CUDA_TRY(cudaMemsetAsync(w.lqueue, 0, size_t(n_epochs) * P * sizeof(uint32_t), st));
   CUBFF_CUDA_TRY(cudaMemsetAsync(w.counters, 0,
                                  size_t(n_epochs) * kPipeCountSlots * 2 * sizeof(unsigned long long), st));
-  CUBFF_CUDA_TRY(cudaMemsetAsync(w.ctl, 0, kPipeCtlWords * sizeof(uint32_t), st));
+  CUBFF_CUDA_TRY(cudaMemsetAsync(w.ctl, 0, 4 * sizeof(uint32_t), st));
   CUBFF_TRY(launch_mutation_masks(s0, first_epoch, n_epochs, n, mutation_prob, w.mutmask, st));
   CUBFF_TRY(launch_inverse(d_shuf_idx, n_epochs, n, w.inv, st));
   PipeBatch b;
@@ -728,7 +675,6 @@ extern "C" int cubff_run_epochs_tuned(int lang, uint8_t *d_programs, const uint3
   sp.n_epochs = n_epochs;
   PipeQueue &q = b.queue;
   q.queue = w.queue;
-  q.lqueue = w.lqueue;
   q.ctl = w.ctl;
   q.total = static_cast<uint32_t>(P * n_epochs);
   q.initial = static_cast<uint32_t>(P);

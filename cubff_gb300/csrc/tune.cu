@@ -3,11 +3,10 @@
 //
 // The reference launches every epoch with one fixed shape: ceil(N/64)
 // blocks of 32 threads, one thread per pair (common_language.h:348,
-// :490-493).  The pipelined launch here has six knobs (cubff_tuning): lanes
+// :490-493).  The pipelined launch here has five knobs (cubff_tuning): lanes
 // in flight per 64 pairs, steps per visit (the first, and the later ones),
-// the claim threshold of busy warps, the visit count after which a pair
-// keeps its warp from claiming, and the lanes of the long warps that take
-// over pairs outlasting their first visit.  The best values depend on the language
+// the claim threshold of busy warps and the visit count after which a pair
+// keeps its warp from claiming.  The best values depend on the language
 // (step cost, how long pairs run), on the number of programs in the launch
 // and on how many soups share it, so the engine keeps one shape per
 // (language, log2 programs, log2 soups) key.
@@ -96,7 +95,6 @@ int tune_language(cubff_engine *eng, std::vector<Clone> &clones, uint32_t epochs
   static const uint32_t kClaim[] = {8, 14, 20, 26, 32};
   static const uint32_t kLong[] = {0, 1, 2, 4, 8};
   static const uint32_t kFirst[] = {4, 8, 16, 32, 64};
-  static const uint32_t kLongLanes[] = {0, 4, 8, 16, 32};
   cubff_tuning best = default_shape();
   Trial warm, ref;
   CUBFF_TRY(run_trial(eng, clones, epochs, best, &warm));  // pairings cached, caches warm
@@ -112,9 +110,9 @@ int tune_language(cubff_engine *eng, std::vector<Clone> &clones, uint32_t epochs
     return CUBFF_OK;
   };
   for (int pass = 0; pass < 2; pass++) {
-    for (int knob = 0; knob < 6; knob++) {
+    for (int knob = 0; knob < 5; knob++) {
       const uint32_t *vals = knob == 0 ? kLanes : knob == 1 ? kSteps : knob == 2 ? kClaim
-                             : knob == 3 ? kLong : knob == 4 ? kFirst : kLongLanes;
+                             : knob == 3 ? kLong : kFirst;
       cubff_tuning round_best = best;
       for (int v = 0; v < 5; v++) {
         cubff_tuning cand = best;
@@ -122,8 +120,7 @@ int tune_language(cubff_engine *eng, std::vector<Clone> &clones, uint32_t epochs
                           : knob == 1 ? &cand.steps_per_visit
                           : knob == 2 ? &cand.claim_min
                           : knob == 3 ? &cand.long_visits
-                          : knob == 4 ? &cand.first_visit_steps
-                                      : &cand.long_lanes;
+                                      : &cand.first_visit_steps;
         *field = vals[v];
         if (same_shape(cand, best)) continue;
         double sec = 0;

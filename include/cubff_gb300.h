@@ -129,9 +129,6 @@ typedef struct {
   uint32_t first_visit_steps; /* steps of a pair's first visit (most pairs end in it; a
                                  small budget keeps one heavy pair from holding the
                                  warp-mates that staged with it)                          */
-  uint32_t long_lanes;        /* > 0: the last warp of every block serves long pairs on
-                                 this many lanes, and a pair still running after its
-                                 first visit elsewhere restarts there (0 = none)          */
 } cubff_tuning;
 
 /* The default launch shape (what a launch uses without a tuned one). */
@@ -284,7 +281,7 @@ uint64_t cubff_soup_footprint_bytes(const cubff_soup_params *params);
  *
  * cubff_engine_tune runs trial_epochs epochs of copies of the given soups
  * (their current bytes and epoch; the soups themselves are not advanced)
- * under candidate shapes, by coordinate descent over the six knobs from the
+ * under candidate shapes, by coordinate descent over the five knobs from the
  * default, checks that every candidate gives the same op counts, and caches
  * the fastest shape for each launch group the soups form.  chosen (nullable,
  * n_soups entries) receives the shape that now applies to each soup.

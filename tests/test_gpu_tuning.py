@@ -27,13 +27,13 @@ def _oracle(lang, n, seed, epochs):
 
 
 SHAPES = [dict(lanes_per_pair64=16, steps_per_visit=16, claim_min=8, long_visits=0,
-               first_visit_steps=16, long_lanes=0),
+               first_visit_steps=16),
           dict(lanes_per_pair64=64, steps_per_visit=256, claim_min=32, long_visits=8,
-               first_visit_steps=4, long_lanes=8),
+               first_visit_steps=4),
           dict(lanes_per_pair64=24, steps_per_visit=1, claim_min=1, long_visits=1,
-               first_visit_steps=1, long_lanes=1),
+               first_visit_steps=1),
           dict(lanes_per_pair64=48, steps_per_visit=128, claim_min=26, long_visits=2,
-               first_visit_steps=8, long_lanes=32)]
+               first_visit_steps=8)]
 
 
 @pytest.mark.parametrize("shape", SHAPES)
