@@ -115,6 +115,11 @@ CRAFTED = {
                     b"+[" + b"q" * 9 + b"<" + b"q" * 5 + b"." + b"q" * 3 + b"]",
                     b"}}}}}}+[<.]" + b"q" * 30, b"+[}}},{{{]", b"+[},]" + b"\x00" * 3 + b"q" * 5,
                     b">>>>+[<<<<<<.>>>>>]",
+                    # bodies that move no head: '+' / '-' and copies on the two bytes
+                    # under the heads, until the byte under h0 is zero (or never)
+                    b"}}}}+[.-]", b"}}+[,-]", b"}}+[.+]", b"}}+[.]", b"+[.]", b"}+[-.+,-]",
+                    b"}}-[..--,]", b"}}}+[-" + b"q" * 9 + b".-]", b"+[.-]", b"{{{{{+[.---]",
+                    b"}}+[,++.+]" + b"q" * 20 + b"+" * 5, b"}}+[+++.]",
                     # a tape that ran 6241 loop iterations of an h1-drift loop
                     bytes.fromhex(
                         "515b7d7b7b7d7d7b807d7d197b7d7d7b7b7d7d7b7b7d7d7b7b7dba7b7b7d7d7b7b7d7d"
@@ -129,6 +134,33 @@ CRAFTED = {
     "subleq": [bytes([5, 6, 0, 0, 0, 0, 0]), bytes([1, 1, 0])],
     "rsubleq4": [bytes([0, 0, 0, 0]), bytes([4, 5, 6, 0xFC])],
 }
+
+
+@pytest.mark.parametrize("lang", [lang for lang in LANGUAGES if lang.startswith("bff")])
+def test_loops_without_head_moves(host_lib, lang):
+    """Random loops whose body moves no head (the register-iterated closed
+    form), with the heads placed anywhere, also inside the loop's code."""
+    rng = np.random.default_rng(3000 + LANGUAGES.index(lang))
+    table = {"bff_perm": {"<": 1, ">": 2, "{": 3, "}": 4, "+": 5, "-": 6, ".": 7, ",": 8,
+                          "[": 9, "]": 10},
+             "bff_noheads_4bit": {c: 16 * 2 + v for c, v in zip("[]+-.,<>{}", range(6, 16))},
+             "bff_selfmove": {">": 0, "<": 1, "+": 2, "-": 3, ",": 4, "[": 5, "]": 6}}
+    enc = table.get(lang, {c: ord(c) for c in "<>{}+-.,[]"})
+    noop = {"bff_perm": 20, "bff_noheads_4bit": 0x31, "bff_selfmove": 20}.get(lang, ord("q"))
+    for trial in range(600):
+        moves = "".join(rng.choice(list("<>{}" if "{" in enc else "<>"), rng.integers(0, 6)))
+        body = "".join(rng.choice([c for c in "+-.," if c in enc], rng.integers(1, 7)))
+        prog = moves + "".join(rng.choice(["+", "-", ""], 1)) + "[" + body + "]"
+        tape = rng.integers(0, 256, 128).astype(np.uint8)
+        if trial % 2:
+            tape[:] = noop
+        start = int(rng.integers(2, 60))
+        for j, ch in enumerate(prog):
+            tape[start + j] = enc[ch] if ch in enc else noop
+        if lang in ("bff", "bff_perm", "bff8", "bff_selfmove"):
+            tape[0] = rng.integers(0, 256)
+            tape[1] = rng.integers(0, 256)
+        check(host_lib, lang, tape)
 
 
 @pytest.mark.parametrize("lang", sorted(CRAFTED))
