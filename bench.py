@@ -348,7 +348,7 @@ def _golden(name: str):
         return json.load(f)["runs"]
 
 
-def batch_compare(torch, abi, epochs: int, peak: float):
+def batch_compare(torch, abi, epochs: int, peak: float, tune_epochs: int = 8):
     """The 64-soup mix (seeds 100..163): all soups in shared pipelined
     launches, one launch group per language on its own stream
     (cubff_batch_run), against one soup at a time (cubff_soup_run), same GPU,
@@ -382,6 +382,12 @@ def batch_compare(torch, abi, epochs: int, peak: float):
     for s in soups:
         s.close()
     soups = make()
+    # The engine's launch-shape tuner picks each language group's shape on
+    # scratch copies of the soups (their state is untouched); the batched run
+    # uses the tuned shapes, the one-at-a-time run the defaults.
+    t0 = time.perf_counter()
+    tuned = eng.tune(soups, trial_epochs=tune_epochs) if tune_epochs else None
+    t_tune = time.perf_counter() - t0
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     bops = abi.batch_run(eng, soups, epochs)
@@ -411,28 +417,37 @@ def batch_compare(torch, abi, epochs: int, peak: float):
             "per_soup_s": t_seq, "batched_s": t_bat,
             "batched_over_per_soup": t_seq / t_bat, "bit_identical": bool(same),
             "bit_identical_vs_reference": vs_ref,
+            "launch_shapes": {
+                "per_soup": "default (cubff_default_tuning)",
+                "batched": ({sp.lang: sh for sp, sh in zip(specs, tuned)} if tuned else "default"),
+                "tuner": (f"cubff_engine_tune, {tune_epochs} trial epochs, {t_tune:.1f} s, "
+                          "outside the timed region") if tuned else None},
             "roofline": {"bound": "int_issue", "achieved": work / t_bat / 1e12,
                          "peak": peak / 1e12, "unit": "T int-instr/s",
                          "frac": work / t_bat / peak,
                          "work": "raw interpreter steps x K_lang of every soup, batched wall time"}}
 
 
-def serving_sample(torch, abi, jobs: int, verify: int = 4):
+def serving_sample(torch, abi, jobs: int, verify: int = 32):
     """The serving stream (Poisson arrivals at 20 jobs/s; job j: seed j, size
     log-uniform in [2^10, 2^17], 64..4096 epochs, language and mutation rate
     as in the batched mix): the first `jobs` jobs replayed in real time
     against a server with a 64 GiB device-memory budget.  A seeded sample of
-    `verify` jobs is re-run alone (cubff_soup_run) and must match."""
+    `verify` jobs is re-run alone (cubff_soup_run) and must match, and the
+    jobs of the committed reference runs (workloads.serving_sample, runs of
+    the reference's own build) must match those runs."""
     import numpy as np
     from cubff_gb300 import serving
-    from cubff_gb300.workloads import serving_jobs
+    from cubff_gb300.workloads import serving_jobs, serving_sample as ref_sample
     arrivals, specs = serving_jobs(jobs)
     rng = np.random.default_rng(11)
     small = [i for i in range(jobs)
              if specs[i].num_programs * specs[i].epochs <= (1 << 14) * 1024]
     check = set(rng.choice(small, size=min(verify, len(small)), replace=False).tolist())
+    ref = _golden("ref_c5.json")
+    ref_ids = [j for j in ref_sample() if j < jobs and f"c5_{j}" in ref] if ref else []
     eng = abi.Engine(0)
-    rep = serving.replay(eng, arrivals, specs, 64 << 30, keep=check)
+    rep = serving.replay(eng, arrivals, specs, 64 << 30, keep=check | set(ref_ids))
     same = True
     for i in sorted(check):
         s = specs[i]
@@ -442,23 +457,33 @@ def serving_sample(torch, abi, jobs: int, verify: int = 4):
         same &= bool(np.array_equal(ops, got_ops) and np.array_equal(soup.read(), got_soup))
         soup.close()
     eng.close()
+    vs_ref = None
+    if ref_ids:
+        vs_ref = True
+        for j in ref_ids:
+            got_soup, got_ops = rep["results"][j]
+            r = ref[f"c5_{j}"]
+            vs_ref &= _sha16(got_soup) == r["sha"][-1] and int(got_ops.sum()) == sum(r["ops"])
     out = serving.summary(rep)
     out.update({"rate_per_s": 20.0, "sample": f"jobs 0..{jobs - 1} of the 2000-job stream",
                 "hbm_budget_gib": 64, "verified_alone": sorted(int(i) for i in check),
-                "same_alone_and_in_mix": same})
+                "same_alone_and_in_mix": same,
+                "verified_vs_reference": sorted(int(j) for j in ref_ids),
+                "same_as_reference_runs": vs_ref})
     return out
 
 
-def cpu_sample(budget_s: float = 20.0, max_epochs: int = 10**9, nthreads: int = 0):
+def cpu_sample(budget_s: float = 20.0, max_epochs: int = 10**9, nthreads: int = 0,
+               min_s: float = 10.0):
     """The reference's CPU implementation (its own build when it was compiled
     on this machine, else the oracle port) on this host's cores: epochs
     0 .. max_epochs-1 of the benchmark workload, the same epochs the GPU arm
-    times, cut short after ~budget_s.  nthreads = 1 times one core (the port
-    only)."""
+    times, cut short after ~budget_s; a sample shorter than min_s is run again
+    from the same start until min_s has passed (the rate is over all passes).
+    nthreads = 1 times one core (the port only)."""
     kind = "port"
     ref_dir = os.path.join(REPO, "oracle", "_ref")
     cores = nthreads or os.cpu_count() or 1
-    ops_total, epochs_run, t_used = 0, 0, 0.0
     refmod = None
     if nthreads == 0:
         try:
@@ -470,21 +495,22 @@ def cpu_sample(budget_s: float = 20.0, max_epochs: int = 10**9, nthreads: int = 
         finally:
             if ref_dir in sys.path:
                 sys.path.remove(ref_dir)
-    if refmod is not None and PATTERN is None:
-        p = refmod.SimulationParams()
-        p.num_programs, p.seed, p.mutation_prob, p.callback_interval = N, SEED, MUT, 1
-        st = {"t0": time.perf_counter(), "ops": 0, "ep": 0}
-
-        def cb(s):
-            st["ops"], st["ep"] = s.total_ops, s.epoch
-            return (time.perf_counter() - st["t0"] > budget_s) or s.epoch >= max_epochs
-        refmod.GetLanguage(LANG).RunSimulation(p, None, cb)
-        t_used = time.perf_counter() - st["t0"]
-        ops_total, epochs_run = st["ops"], st["ep"]
-    else:
+    if refmod is None or PATTERN is not None:
         from oracle import oracle as O
         kind = "port"
         O.build()
+
+    def one_pass():
+        if kind == "reference":
+            p = refmod.SimulationParams()
+            p.num_programs, p.seed, p.mutation_prob, p.callback_interval = N, SEED, MUT, 1
+            st = {"t0": time.perf_counter(), "ops": 0, "ep": 0}
+
+            def cb(s):
+                st["ops"], st["ep"] = s.total_ops, s.epoch
+                return (time.perf_counter() - st["t0"] > budget_s) or s.epoch >= max_epochs
+            refmod.GetLanguage(LANG).RunSimulation(p, None, cb)
+            return st["ops"], st["ep"], time.perf_counter() - st["t0"]
         t0 = time.perf_counter()
         st = {"ops": 0, "ep": 0}
 
@@ -498,12 +524,20 @@ def cpu_sample(budget_s: float = 20.0, max_epochs: int = 10**9, nthreads: int = 
             from cubff_gb300.workloads import grid_pattern
             O.OracleSim(LANG, N, SEED, MUT, pairing=O.PAIR_PATTERN,
                         pattern=grid_pattern(*PATTERN), nthreads=nthreads).run(cb)
-        t_used = time.perf_counter() - t0
-        ops_total, epochs_run = st["ops"], st["ep"]
+        return st["ops"], st["ep"], time.perf_counter() - t0
+
+    ops_total, epochs_run, t_used = one_pass()
+    passes = 1
+    while t_used < min_s and epochs_run >= max_epochs:
+        o, _, t = one_pass()
+        ops_total += o
+        t_used += t
+        passes += 1
     return {"value": ops_total / t_used, "unit": "steps/s", "cores": cores, "kind": kind,
             "epochs": epochs_run,
-            "sample": f"{LANG} {_log2(N)} programs seed {SEED}, epochs 0..{epochs_run - 1} "
-                      f"({t_used:.1f} s, callback per epoch)"}
+            "sample": f"{LANG} {_log2(N)} programs seed {SEED}, epochs 0..{epochs_run - 1}"
+                      f"{f' x {passes} passes' if passes > 1 else ''} ({t_used:.1f} s, "
+                      "callback per epoch)"}
 
 
 def post_emergence(torch, abi, peak: float, start: int = 5121, epochs: int = 256,
@@ -662,6 +696,7 @@ def main():
             "raw_steps_per_s": raw_all / t_dev,
             "pairs_per_s": (N // 2) * args.steps * world / t_dev,
             "gpu_launches": gv["launches"],
+            "launch_shape": dict(abi.default_tuning(), source="default (cubff_default_tuning)"),
             "roofline": roofline(gv, peaks, src, peak, peak_detail),
             "clocks": ck,
             "e2e": {"value": ops_e2e / t_e2e, "unit": "steps/s",

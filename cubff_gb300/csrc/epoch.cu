@@ -9,6 +9,7 @@
 // op count is reduced per warp (redux) and added with one atomic per warp, as
 // IncreaseInsnCount does (common_language.h:56-63).
 #include <algorithm>
+#include <atomic>
 #include "internal.h"
 #include "epoch_body.cuh"
 
@@ -97,12 +98,12 @@ int launch_epoch_t(const EpochArgs &a, cudaStream_t stream) {
   const uint64_t npairs = a.n / 2;
   if (npairs == 0) return CUBFF_OK;
   const size_t smem = epoch_smem_bytes<L>();
-  static bool attr_set = false;  // per-process; benign race (idempotent)
-  if (!attr_set) {
+  static std::atomic<bool> attr_set{false};  // per process; setting it twice is harmless
+  if (!attr_set.load()) {
     CUBFF_CUDA_TRY(cudaFuncSetAttribute(epoch_kernel<L>,
                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         static_cast<int>(smem)));
-    attr_set = true;
+    attr_set.store(true);
   }
   const uint64_t grid = (npairs + kThreads - 1) / kThreads;
   epoch_kernel<L><<<static_cast<unsigned>(grid), kThreads, smem, stream>>>(a);

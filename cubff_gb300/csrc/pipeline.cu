@@ -445,21 +445,21 @@ __global__ void __launch_bounds__(kThreads, (L <= kBffSelfmove) ? 3 : 4)
 template <int L>
 int launch_pipeline_t(const PipeBatch &b, uint64_t total_pairs, uint32_t lanes_per_pair64,
                       int device, cudaStream_t stream) {
-  static int sms_cache[64] = {0};
+  static std::atomic<int> sms_cache[64];  // (zero-initialised: static storage)
   const size_t smem_max = pipeline_smem_bytes<L>(kMaxPipeSoups);
-  if (sms_cache[device & 63] == 0) {
+  if (sms_cache[device & 63].load() == 0) {
     CUBFF_CUDA_TRY(cudaFuncSetAttribute(pipeline_kernel<L>,
                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         static_cast<int>(smem_max)));
     int sms = 0;
     CUBFF_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
-    sms_cache[device & 63] = sms;
+    sms_cache[device & 63].store(sms);
   }
   const size_t smem = pipeline_smem_bytes<L>(b.n_soups);
   int per_sm = 0;
   CUBFF_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, pipeline_kernel<L>,
                                                                kThreads, smem));
-  const uint64_t resident = uint64_t(std::max(1, per_sm)) * sms_cache[device & 63];
+  const uint64_t resident = uint64_t(std::max(1, per_sm)) * sms_cache[device & 63].load();
   // Lanes in flight: enough to keep the SMs busy, few enough that most held
   // pairs are ready (a lane holding a pair of a later epoch only polls).
   // lanes_per_pair64 (x1/64) is tunable; the default keeps half an epoch of

@@ -1,17 +1,23 @@
 // server.cu — serving soup jobs (cubff_server_*): continuous admission by
 // device-memory footprint and batched advancement of the running jobs.
 //
-// One worker thread owns the engine.  Each round it
-//   1. admits queued jobs in submission order while the running jobs'
-//      summed footprint stays within the budget (the head of the queue is
-//      never skipped, so a large job cannot starve),
-//   2. advances every running job by min(round_epochs, the epochs it has
-//      left) in one run_soups call (pipelined launches shared by all running
+// One worker thread per language, each with an engine of its own (its own
+// streams and launch buffers, on the server's device), serves the jobs of
+// that language.  Each round a worker
+//   1. admits the queued jobs of its language in submission order while the
+//      summed footprint of all running jobs stays within the budget (a job
+//      of its language that does not fit is not skipped, so a large job
+//      cannot starve behind smaller ones of the same language),
+//   2. advances every job it runs by min(round_epochs, the epochs it has
+//      left) in one run_soups call (pipelined launches shared by its running
 //      jobs; a job near its end does not shorten the others' round),
 //   3. retires the jobs that are done: soup bytes and op counts to the host,
 //      device memory released.
-// A job's results equal cubff_soup_run's for the same parameters: run_soups
-// gives every soup exactly its own epoch sequence.
+// The workers run side by side, so a job that arrives while other
+// languages' rounds are on the GPU starts at once, its launches overlapping
+// theirs; within a language it joins at the next round.  A job's results
+// equal cubff_soup_run's for the same parameters: run_soups gives every soup
+// exactly its own epoch sequence.
 #include <chrono>
 #include <condition_variable>
 #include <deque>
@@ -42,53 +48,71 @@ double seconds_since(std::chrono::steady_clock::time_point t0) {
   return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
 }
 
+// The worker of one language.
+struct LangWorker {
+  int lang = 0;
+  cubff_engine *eng = nullptr;                     // created by the worker
+  std::vector<std::unique_ptr<Job>> running;       // worker only
+  std::thread th;
+};
+
 }  // namespace
 
 struct cubff_server {
-  cubff_engine *eng = nullptr;
+  cubff_engine *eng = nullptr;  // the caller's engine: gives the device
   uint64_t budget = 0;
   uint32_t round_epochs = 64;
   std::chrono::steady_clock::time_point t0;
 
   std::mutex mu;
-  std::condition_variable work_cv;  // the worker waits for jobs
+  std::condition_variable work_cv;  // workers wait for jobs or budget
   std::condition_variable done_cv;  // pollers wait for finished jobs
   bool stop = false;
   uint64_t next_id = 1;
   std::deque<std::unique_ptr<Job>> queued;           // guarded by mu
-  std::vector<std::unique_ptr<Job>> running;         // worker only
-  uint64_t n_running = 0, running_bytes = 0;         // guarded by mu (copies for stats)
+  uint64_t n_running = 0, running_bytes = 0;         // guarded by mu
   std::map<uint64_t, std::unique_ptr<Job>> finished; // guarded by mu
   std::deque<uint64_t> unreported;                   // finished ids not yet polled
-  std::thread worker;
+  std::unique_ptr<LangWorker> workers[cubff::kNumLangs];  // created on a language's first job
 
-  void loop();
-  void admit();
+  void loop(LangWorker *w);
+  // True (mu held) when the first queued job of lang fits the budget.
+  bool admissible(int lang) const;
+  void admit(LangWorker *w);
   void retire(std::unique_ptr<Job> job, int status);
 };
 
-void cubff_server::admit() {
+bool cubff_server::admissible(int lang) const {
+  for (const auto &j : queued)
+    if (j->params.lang == lang) return running_bytes + j->footprint <= budget;
+  return false;
+}
+
+void cubff_server::admit(LangWorker *w) {
   std::vector<std::unique_ptr<Job>> take;
   {
     std::lock_guard<std::mutex> lk(mu);
-    uint64_t bytes = running_bytes;
-    while (!queued.empty() && bytes + queued.front()->footprint <= budget) {
-      bytes += queued.front()->footprint;
-      take.push_back(std::move(queued.front()));
-      queued.pop_front();
+    for (auto it = queued.begin(); it != queued.end();) {
+      if ((*it)->params.lang != w->lang) {
+        ++it;
+        continue;
+      }
+      if (running_bytes + (*it)->footprint > budget) break;  // not skipped
+      running_bytes += (*it)->footprint;
+      take.push_back(std::move(*it));
+      it = queued.erase(it);
     }
-    running_bytes = bytes;
     n_running += take.size();
   }
   for (auto &job : take) {
     job->start_s = seconds_since(t0);
-    int st = cubff_soup_create(eng, &job->params, &job->soup);
+    int st = cubff_soup_create(w->eng, &job->params, &job->soup);
     if (st == CUBFF_OK) st = job->soup->ensure_buffers();
     if (st != CUBFF_OK) {
       retire(std::move(job), st);
       continue;
     }
-    running.push_back(std::move(job));
+    w->running.push_back(std::move(job));
   }
 }
 
@@ -101,44 +125,42 @@ void cubff_server::retire(std::unique_ptr<Job> job, int status) {
   if (job->soup) cubff_soup_destroy(job->soup);
   job->soup = nullptr;
   job->finish_s = seconds_since(t0);
-  std::lock_guard<std::mutex> lk(mu);
-  if (n_running) n_running--;
-  running_bytes -= std::min(running_bytes, job->footprint);
-  unreported.push_back(job->id);
-  finished[job->id] = std::move(job);
+  {
+    std::lock_guard<std::mutex> lk(mu);
+    if (n_running) n_running--;
+    running_bytes -= std::min(running_bytes, job->footprint);
+    unreported.push_back(job->id);
+    finished[job->id] = std::move(job);
+  }
   done_cv.notify_all();
+  work_cv.notify_all();  // budget freed: other workers may admit
 }
 
-void cubff_server::loop() {
+void cubff_server::loop(LangWorker *w) {
   cudaSetDevice(eng->device);
   while (true) {
     {
       std::unique_lock<std::mutex> lk(mu);
-      work_cv.wait(lk, [&] { return stop || !queued.empty() || !running.empty(); });
+      work_cv.wait(lk, [&] { return stop || !w->running.empty() || admissible(w->lang); });
       if (stop) break;
     }
-    admit();
-    if (running.empty()) {
-      // The queue head does not fit although nothing runs: cannot happen,
-      // submit rejects jobs larger than the budget.
-      std::this_thread::sleep_for(std::chrono::milliseconds(1));
-      continue;
-    }
+    admit(w);
+    if (w->running.empty()) continue;
     // Every job advances by its own quantum: round_epochs, or what it has
     // left (a job about to finish does not shorten the others' round).
     std::vector<cubff_soup *> soups;
     std::vector<uint64_t *> ops;
     std::vector<uint64_t> quantum;
-    for (auto &j : running) {
+    for (auto &j : w->running) {
       soups.push_back(j->soup);
       ops.push_back(j->ops.data() + j->done);
       quantum.push_back(std::min<uint64_t>(round_epochs, j->n_epochs - j->done));
     }
-    const int st = cubff::run_soups(eng, soups.data(), static_cast<int>(soups.size()), round_epochs,
-                                    ops.data(), nullptr, nullptr, quantum.data());
+    const int st = cubff::run_soups(w->eng, soups.data(), static_cast<int>(soups.size()),
+                                    round_epochs, ops.data(), nullptr, nullptr, quantum.data());
     std::vector<std::unique_ptr<Job>> keep;
-    for (size_t q = 0; q < running.size(); q++) {
-      auto &j = running[q];
+    for (size_t q = 0; q < w->running.size(); q++) {
+      auto &j = w->running[q];
       if (st != CUBFF_OK) {
         retire(std::move(j), st);
         continue;
@@ -147,11 +169,11 @@ void cubff_server::loop() {
       if (j->done == j->n_epochs) retire(std::move(j), CUBFF_OK);
       else keep.push_back(std::move(j));
     }
-    running.swap(keep);
+    w->running.swap(keep);
   }
-  for (auto &j : running)
+  for (auto &j : w->running)
     if (j->soup) cubff_soup_destroy(j->soup);
-  running.clear();
+  w->running.clear();
 }
 
 using namespace cubff;
@@ -168,7 +190,6 @@ int cubff_server_create(cubff_engine *engine, uint64_t hbm_budget_bytes, uint32_
   s->budget = hbm_budget_bytes;
   s->round_epochs = round_epochs ? round_epochs : 64;
   s->t0 = std::chrono::steady_clock::now();
-  s->worker = std::thread([s] { s->loop(); });
   *out = s;
   return CUBFF_OK;
 }
@@ -180,7 +201,11 @@ int cubff_server_destroy(cubff_server *s) {
     s->stop = true;
   }
   s->work_cv.notify_all();
-  if (s->worker.joinable()) s->worker.join();
+  for (auto &w : s->workers) {
+    if (!w) continue;
+    if (w->th.joinable()) w->th.join();
+    if (w->eng) cubff_engine_destroy(w->eng);
+  }
   delete s;
   return CUBFF_OK;
 }
@@ -209,11 +234,23 @@ int cubff_server_submit(cubff_server *s, const cubff_soup_params *params, uint64
   job->submit_s = seconds_since(s->t0);
   {
     std::lock_guard<std::mutex> lk(s->mu);
+    if (!s->workers[p.lang]) {
+      auto w = std::make_unique<LangWorker>();
+      w->lang = p.lang;
+      int prev = 0;  // engine creation makes its device current: keep the caller's
+      cudaGetDevice(&prev);
+      const int st = cubff_engine_create(s->eng->device, &w->eng);
+      cudaSetDevice(prev);
+      if (st != CUBFF_OK) return st;
+      LangWorker *wp = w.get();
+      w->th = std::thread([s, wp] { s->loop(wp); });
+      s->workers[p.lang] = std::move(w);
+    }
     job->id = s->next_id++;
     if (job_id) *job_id = job->id;
     s->queued.push_back(std::move(job));
   }
-  s->work_cv.notify_one();
+  s->work_cv.notify_all();
   return CUBFF_OK;
 }
 
