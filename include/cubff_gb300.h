@@ -308,14 +308,17 @@ int cubff_batch_run(cubff_engine *engine, cubff_soup **soups, int n_soups,
 
 /* ---- layer 4: serving -------------------------------------------------- */
 /* A server runs soup jobs (parameters + epoch count) submitted at any time.
- * A worker thread admits queued jobs in submission order while the summed
- * footprint (cubff_soup_footprint_bytes) of the running jobs stays within
- * hbm_budget_bytes, advances all running jobs together (cubff_batch_run) in
- * rounds of at most round_epochs epochs, and retires finished jobs: their
- * final soup and per-epoch op counts are kept on the host until fetched.  A
- * job's results are the same as cubff_soup_run's on a soup created with the
- * same parameters.  The worker owns the engine: do not use the engine, or
- * its soups, while the server exists. */
+ * Each language has a worker thread with an engine of its own (created on
+ * the given engine's device at the language's first job).  A worker admits
+ * the queued jobs of its language in submission order while the summed
+ * footprint (cubff_soup_footprint_bytes) of all running jobs stays within
+ * hbm_budget_bytes, advances its running jobs together (as cubff_batch_run
+ * does) in rounds in which each job takes min(round_epochs, its epochs left),
+ * and retires finished jobs: their final soup and per-epoch op counts are
+ * kept on the host until fetched.  The workers run side by side, so the
+ * rounds of one language do not wait for another's.  A job's results are the
+ * same as cubff_soup_run's on a soup created with the same parameters.  The
+ * given engine only names the device; it stays usable. */
 typedef struct cubff_server cubff_server;
 
 typedef struct {
@@ -332,7 +335,7 @@ typedef struct {
 /* round_epochs = 0 picks 64. */
 int cubff_server_create(cubff_engine *engine, uint64_t hbm_budget_bytes,
                         uint32_t round_epochs, cubff_server **out);
-/* Stops the worker after its current round; unfinished jobs are dropped. */
+/* Stops the workers after their current rounds; unfinished jobs are dropped. */
 int cubff_server_destroy(cubff_server *server);
 /* Queues a job.  CUBFF_EINVAL for bad parameters or a job whose footprint
  * alone exceeds the budget.  Pattern pairing is not served. */
