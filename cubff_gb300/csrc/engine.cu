@@ -80,6 +80,9 @@ int cubff_soup::ensure_buffers() {
     CUBFF_CUDA_TRY(cudaMalloc(&d_mutmask, size_t(batch) * (p.num_programs / 2) * sizeof(uint4)));
     CUBFF_CUDA_TRY(cudaMalloc(&d_inv, size_t(batch) * p.num_programs * sizeof(uint32_t)));
     CUBFF_CUDA_TRY(cudaMalloc(&d_readycnt, size_t(batch) * (p.num_programs / 2) * sizeof(uint32_t)));
+    CUBFF_CUDA_TRY(cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking));
+    CUBFF_CUDA_TRY(cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming));
+    CUBFF_CUDA_TRY(cudaEventCreateWithFlags(&ev_join, cudaEventDisableTiming));
     // On the engine's stream, which every pipelined launch follows (the
     // legacy default stream would not order it before them).
     CUBFF_CUDA_TRY(cudaMemsetAsync(d_readycnt, 0,
@@ -113,6 +116,11 @@ void cubff_soup::release() {
   d_mutmask = nullptr;
   if (d_hist) cudaFree(d_hist);
   d_hist = nullptr;
+  if (side) cudaStreamDestroy(side);
+  if (ev_fork) cudaEventDestroy(ev_fork);
+  if (ev_join) cudaEventDestroy(ev_join);
+  side = nullptr;
+  ev_fork = ev_join = nullptr;
   d_soup = nullptr;
   d_perm = nullptr;
   d_num_indices = nullptr;
@@ -124,6 +132,14 @@ void cubff_soup::release() {
 // Computes the pairing of epochs [first, first + count) into d_perm.
 int cubff_soup::fill_pairing(uint64_t first, uint32_t count, cudaStream_t st) {
   const uint64_t n = p.num_programs;
+  if (p.pairing == CUBFF_PAIR_PATTERN && !d_pat_offs)
+    return set_error(CUBFF_EINVAL, "pattern pairing without interaction lists");
+  // Mutation masks on the side stream, after everything queued on st so far
+  // (the previous launch still reads the old masks), beside the pairing.
+  CUBFF_CUDA_TRY(cudaEventRecord(ev_fork, st));
+  CUBFF_CUDA_TRY(cudaStreamWaitEvent(side, ev_fork, 0));
+  CUBFF_TRY(launch_mutation_masks(s0, first, count, n, p.mutation_prob, d_mutmask, side));
+  CUBFF_CUDA_TRY(cudaEventRecord(ev_join, side));
   switch (p.pairing) {
     case CUBFF_PAIR_SHUFFLE:
       CUBFF_TRY(launch_shuffle(s0, first, count, n, d_perm, d_scratch, st));
@@ -135,8 +151,6 @@ int cubff_soup::fill_pairing(uint64_t first, uint32_t count, cudaStream_t st) {
       CUBFF_TRY(launch_cyclic(first, count, n, d_perm, st));
       break;
     case CUBFF_PAIR_PATTERN:
-      if (!d_pat_offs)
-        return set_error(CUBFF_EINVAL, "pattern pairing without interaction lists");
       CUBFF_TRY(launch_pattern(s0, first, count, n, d_pat_offs, d_pat_tgts, d_perm, d_num_indices,
                                d_scratch, h_pat_undecided, st));
       CUBFF_CUDA_TRY(cudaMemcpyAsync(h_pat_ni, d_num_indices, size_t(count) * sizeof(uint64_t),
@@ -146,8 +160,8 @@ int cubff_soup::fill_pairing(uint64_t first, uint32_t count, cudaStream_t st) {
     default:
       return set_error(CUBFF_EINVAL, "unknown pairing mode %d", p.pairing);
   }
-  CUBFF_TRY(launch_mutation_masks(s0, first, count, n, p.mutation_prob, d_mutmask, st));
   CUBFF_TRY(launch_inverse(d_perm, count, n, d_inv, st));
+  CUBFF_CUDA_TRY(cudaStreamWaitEvent(st, ev_join, 0));
   perm_first = first;
   perm_count = count;
   return CUBFF_OK;

@@ -66,6 +66,11 @@ struct cubff_soup {
   uint32_t *d_readycnt = nullptr;  // [batch][num_programs / 2] ready-queue input counts
   uint4 *d_mutmask = nullptr;      // [batch][num_programs / 2] mutation masks
 
+  // The mutation masks depend on the epochs only: fill_pairing computes them
+  // on this side stream while the pairing kernels run, joined before use.
+  cudaStream_t side = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+
   bool dirty = false;              // a launch gave up: d_readycnt may be nonzero
   unsigned long long *d_hist = nullptr;  // [256] byte counts (cubff_soup_histogram)
 

@@ -53,24 +53,56 @@ __global__ void fy_draw(uint64_t s0, uint64_t first_epoch, uint64_t n, uint64_t 
   atomicAdd(&cnt[e * n + ji], 1u);
 }
 
-// Exclusive scan of cnt per epoch segment into start; cnt is then zeroed for
-// reuse as the fill cursor.  One 1024-thread block per epoch.
-__global__ void __launch_bounds__(1024) fy_scan(uint64_t n, uint32_t *cnt, uint32_t *start) {
-  __shared__ uint32_t warp_sums[32];
-  __shared__ uint32_t carry_s;
-  const uint64_t off = uint64_t(blockIdx.x) * n;
-  uint32_t *c = cnt + off;
-  uint32_t *s = start + off;
-  const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  if (tid == 0) carry_s = 0;
+// Exclusive scan of cnt per epoch segment into start (cnt is then zeroed for
+// reuse as the fill cursor), in chunks of kScanChunk counts: one 1024-thread
+// block per (chunk, epoch) sums its chunk, then one per (chunk, epoch) adds
+// the sums of the epoch's earlier chunks to its own in-chunk scan.
+constexpr uint32_t kScanChunk = 4096;
+
+__device__ __forceinline__ uint32_t block_sum_1024(uint32_t v, uint32_t *warp_sums) {
+  const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  v = __reduce_add_sync(0xffffffffu, v);
+  if (lane == 0) warp_sums[warp] = v;
   __syncthreads();
-  for (uint64_t base = 0; base < n; base += 4096) {
-    uint32_t v[4];
-    uint32_t sum = 0;
+  uint32_t t = warp_sums[lane];
+  t = __reduce_add_sync(0xffffffffu, t);
+  __syncthreads();
+  return t;
+}
+
+__global__ void __launch_bounds__(1024) fy_chunk_sums(uint64_t n, uint32_t E, uint32_t chunks,
+                                                      const uint32_t *cnt, uint32_t *sums) {
+  __shared__ uint32_t warp_sums[32];
+  const uint32_t c = blockIdx.x;
+  for (uint32_t e = blockIdx.y; e < E; e += gridDim.y) {
+    const uint32_t *ce = cnt + uint64_t(e) * n;
+    const uint64_t x0 = uint64_t(c) * kScanChunk + threadIdx.x * 4;
+    uint32_t v = 0;
+#pragma unroll
+    for (int q = 0; q < 4; q++)
+      if (x0 + q < n) v += ce[x0 + q];
+    const uint32_t t = block_sum_1024(v, warp_sums);
+    if (threadIdx.x == 0) sums[uint64_t(e) * chunks + c] = t;
+  }
+}
+
+__global__ void __launch_bounds__(1024) fy_chunk_scan(uint64_t n, uint32_t E, uint32_t chunks,
+                                                      uint32_t *cnt, uint32_t *start,
+                                                      const uint32_t *sums) {
+  __shared__ uint32_t warp_sums[32];
+  const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, c = blockIdx.x;
+  for (uint32_t e = blockIdx.y; e < E; e += gridDim.y) {
+    // The sums of the epoch's chunks before this one.
+    uint32_t before = 0;
+    for (uint32_t q = tid; q < c; q += 1024) before += sums[uint64_t(e) * chunks + q];
+    const uint32_t carry = block_sum_1024(before, warp_sums);
+    uint32_t *ce = cnt + uint64_t(e) * n;
+    uint32_t *se = start + uint64_t(e) * n;
+    const uint64_t x0 = uint64_t(c) * kScanChunk + tid * 4;
+    uint32_t v[4], sum = 0;
 #pragma unroll
     for (int q = 0; q < 4; q++) {
-      const uint64_t x = base + tid * 4 + q;
-      v[q] = x < n ? c[x] : 0;
+      v[q] = x0 + q < n ? ce[x0 + q] : 0;
       sum += v[q];
     }
     uint32_t incl = sum;
@@ -82,7 +114,7 @@ __global__ void __launch_bounds__(1024) fy_scan(uint64_t n, uint32_t *cnt, uint3
     if (lane == 31) warp_sums[warp] = incl;
     __syncthreads();
     if (warp == 0) {
-      uint32_t ws = warp_sums[lane];
+      const uint32_t ws = warp_sums[lane];
       uint32_t wi = ws;
 #pragma unroll
       for (int d = 1; d < 32; d <<= 1) {
@@ -92,20 +124,27 @@ __global__ void __launch_bounds__(1024) fy_scan(uint64_t n, uint32_t *cnt, uint3
       warp_sums[lane] = wi - ws;  // exclusive prefix of warps
     }
     __syncthreads();
-    uint32_t run = carry_s + warp_sums[warp] + incl - sum;
+    uint32_t run = carry + warp_sums[warp] + incl - sum;
 #pragma unroll
     for (int q = 0; q < 4; q++) {
-      const uint64_t x = base + tid * 4 + q;
-      if (x < n) {
-        s[x] = run;
-        c[x] = 0;
+      if (x0 + q < n) {
+        se[x0 + q] = run;
+        ce[x0 + q] = 0;
       }
       run += v[q];
     }
-    __syncthreads();
-    if (tid == 1023) carry_s = run;
-    __syncthreads();
+    __syncthreads();  // warp_sums is reused by the next epoch
   }
+}
+
+// Exclusive scan of E segments of n counts (cnt -> start, cnt zeroed); sums
+// holds E * ceil(n / kScanChunk) words of scratch.
+void launch_segment_scan(uint64_t n, uint32_t E, uint32_t *cnt, uint32_t *start, uint32_t *sums,
+                         cudaStream_t stream) {
+  const uint64_t chunks = (n + kScanChunk - 1) / kScanChunk;
+  const dim3 grid(static_cast<unsigned>(chunks), E < 65535u ? E : 65535u);
+  fy_chunk_sums<<<grid, 1024, 0, stream>>>(n, E, static_cast<uint32_t>(chunks), cnt, sums);
+  fy_chunk_scan<<<grid, 1024, 0, stream>>>(n, E, static_cast<uint32_t>(chunks), cnt, start, sums);
 }
 
 __global__ void fy_fill(uint64_t n, uint64_t m, const uint32_t *j, uint32_t *cnt,
@@ -364,7 +403,8 @@ int launch_pattern(uint64_t s0, uint64_t first_epoch, uint32_t E, uint64_t n,
   pat_propose<<<blocks, 256, 0, stream>>>(s0, first_epoch, n, m, offs, tgts, nb, cnt, status);
   // In-degree counts -> lists: len keeps the counts, start their prefix sums.
   CUBFF_CUDA_TRY(cudaMemcpyAsync(len, cnt, m * sizeof(uint32_t), cudaMemcpyDeviceToDevice, stream));
-  fy_scan<<<E, 1024, 0, stream>>>(n, cnt, start);  // (also zeroes cnt)
+  // (also zeroes cnt; the chunk sums go to the shuffle's scratch, free by now)
+  launch_segment_scan(n, E, cnt, start, static_cast<uint32_t *>(fy), stream);
   pat_fill<<<blocks, 256, 0, stream>>>(n, m, nb, cnt, start, bucket);
   // Rounds until every edge is decided (checked every 8 rounds).
   for (int checks = 0;; checks++) {
@@ -383,9 +423,10 @@ int launch_pattern(uint64_t s0, uint64_t first_epoch, uint32_t E, uint64_t n,
   }
   pat_flags<<<blocks, 256, 0, stream>>>(n, m, order, nb, status, used);
   pat_count<<<blocks, 256, 0, stream>>>(n, m, order, status, used, acc, unused);
-  // Exclusive prefix sums per epoch (in place: fy_scan reads cnt, writes start, zeroes cnt).
-  fy_scan<<<E, 1024, 0, stream>>>(n, acc, start);
-  fy_scan<<<E, 1024, 0, stream>>>(n, unused, len);
+  // Exclusive prefix sums per epoch (each scan reads its counts, writes the
+  // sums, zeroes the counts).
+  launch_segment_scan(n, E, acc, start, static_cast<uint32_t *>(fy), stream);
+  launch_segment_scan(n, E, unused, len, static_cast<uint32_t *>(fy), stream);
   pat_write<<<blocks, 256, 0, stream>>>(n, m, order, nb, status, used, start, len, out, num_indices);
   CUBFF_CUDA_TRY(cudaGetLastError());
   return CUBFF_OK;
@@ -406,7 +447,8 @@ int launch_shuffle(uint64_t s0, uint64_t first_epoch, uint32_t E, uint64_t n,
   FyBufs b = fy_bufs(scratch, n, E);
   CUBFF_CUDA_TRY(cudaMemsetAsync(b.cnt, 0, m * sizeof(uint32_t), stream));
   fy_draw<<<blocks_for(m, 256), 256, 0, stream>>>(s0, first_epoch, n, m, b.j, b.cnt);
-  fy_scan<<<E, 1024, 0, stream>>>(n, b.cnt, b.start);
+  // The chunk sums live in nxt until fy_link writes it.
+  launch_segment_scan(n, E, b.cnt, b.start, reinterpret_cast<uint32_t *>(b.nxt), stream);
   fy_fill<<<blocks_for(m, 256), 256, 0, stream>>>(n, m, b.j, b.cnt, b.start, b.bucket);
   fy_link<<<blocks_for(m, 256), 256, 0, stream>>>(n, m, b.j, b.cnt, b.start, b.bucket,
                                                   b.nxt, b.par);
