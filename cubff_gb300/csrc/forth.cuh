@@ -5,7 +5,7 @@
 // Evaluate (forth.inc.h:379-397); forthtrivial_reset's Reset / ResetIf and its
 // Write1 / Copy0 (forthtrivial_reset.cu:58-72, :157-166, :215-223).  The
 // stack (128 bytes) lives in shared memory in the same bank-per-lane layout as
-// the tape.
+// the tape, its top two entries in registers (ForthMachine).
 //
 // Exact cycle fast-forward at backward jumps (Brent's schedule, as in
 // cycle.cuh): the state is (pos, stack pointer, stack contents, tape).  The
@@ -30,10 +30,16 @@ static __host__ __device__ __noinline__ void forth_reset(const LaneBytes t, int 
                                               static_cast<uint64_t>(i))));
 }
 
+// The top two stack entries live in registers (r0 = stack[sp - 1], r1 =
+// stack[sp - 2]); shared memory holds stack[0 .. sp - 2).  Most ops then
+// touch no memory for their stack traffic: a push spills the entry it
+// pushes down, a pop refills the second entry, neither on the step's own
+// dependency chain.
 template <bool kWithReset>
 struct ForthMachine {
   int pos, sp;
   bool overflow;
+  uint32_t r0, r1;         // stack[sp - 1], stack[sp - 2] (when they exist)
   uint32_t i, nops, mods;  // mods: value-changing tape writes
   // Brent-schedule snapshot taken at a backward jump.
   int s_pos, s_sp;
@@ -45,6 +51,7 @@ struct ForthMachine {
   __host__ __device__ __forceinline__ void begin() {
     pos = sp = 0;
     overflow = false;
+    r0 = r1 = 0;
     i = nops = mods = 0;
     s_pos = -1;
     s_sp = 0;
@@ -56,7 +63,9 @@ struct ForthMachine {
 
   __host__ __device__ __forceinline__ void push(const LaneBytes stk, uint32_t v) {
     if (sp != kPair) {
-      stk.set(sp, v & 0xFF);
+      if (sp >= 2) stk.set(sp - 2, r1);
+      r1 = r0;
+      r0 = v & 0xFF;
       sp++;
     } else {
       overflow = true;
@@ -65,7 +74,9 @@ struct ForthMachine {
 
   __host__ __device__ __forceinline__ uint64_t pack_stack(const LaneBytes stk) const {
     uint64_t w = 0;
-    for (int j = 0; j < sp; j++) w |= static_cast<uint64_t>(stk.get(j)) << (8 * j);
+    for (int j = 0; j < sp - 2; j++) w |= static_cast<uint64_t>(stk.get(j)) << (8 * j);
+    if (sp >= 2) w |= static_cast<uint64_t>(r1) << (8 * (sp - 2));
+    if (sp >= 1) w |= static_cast<uint64_t>(r0) << (8 * (sp - 1));
     return w;
   }
 
@@ -92,7 +103,12 @@ struct ForthMachine {
     }
   }
   __host__ __device__ __forceinline__ uint32_t pop(const LaneBytes stk) {
-    return sp == 0 ? 0u : stk.get(--sp);
+    if (sp == 0) return 0u;
+    const uint32_t v = r0;
+    sp--;
+    r0 = r1;
+    if (sp >= 2) r1 = stk.get(sp - 2);
+    return v;
   }
   __host__ __device__ __forceinline__ void write(const LaneBytes t, int a, uint32_t v) {
     v &= 0xFF;
