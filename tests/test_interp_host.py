@@ -163,6 +163,48 @@ def test_loops_without_head_moves(host_lib, lang):
         check(host_lib, lang, tape)
 
 
+@pytest.mark.parametrize("lang", [lang for lang in LANGUAGES if lang.startswith("bff")])
+def test_copy_loops_with_moving_heads(host_lib, lang):
+    """Random loops whose body is one copy among head moves (the copy loops of
+    self-replicators, taken in a tight loop over positions), with the heads
+    anywhere: overlapping source and destination, inside the loop's code,
+    crossing the tape's end."""
+    rng = np.random.default_rng(5000 + LANGUAGES.index(lang))
+    table = {"bff_perm": {"<": 1, ">": 2, "{": 3, "}": 4, "+": 5, "-": 6, ".": 7, ",": 8,
+                          "[": 9, "]": 10},
+             "bff_noheads_4bit": {c: 16 * 2 + v for c, v in zip("[]+-.,<>{}", range(6, 16))},
+             "bff_selfmove": {">": 0, "<": 1, "+": 2, "-": 3, ",": 4, "[": 5, "]": 6}}
+    enc = table.get(lang, {c: ord(c) for c in "<>{}+-.,[]"})
+    noop = {"bff_perm": 20, "bff_noheads_4bit": 0x31, "bff_selfmove": 20}.get(lang, ord("q"))
+    moves = [c for c in "<>{}" if c in enc]
+    copies = [c for c in ".," if c in enc]
+    for trial in range(800):
+        pre = "".join(rng.choice(moves, rng.integers(0, 3)))
+        post = "".join(rng.choice(moves, rng.integers(1, 4)))
+        copy = rng.choice(copies) * int(rng.integers(1, 3))
+        body = pre + copy + post
+        lead = "".join(rng.choice(moves, rng.integers(0, 8)))
+        prog = lead + "+[" + body + "]"
+        tape = rng.integers(0, 256, 128).astype(np.uint8)
+        if trial % 3 == 0:
+            tape[:] = noop
+            tape[rng.integers(0, 128, 3)] = 0
+        elif trial % 3 == 1:
+            tape[tape == 0] = 1  # no zero: the loop runs to the step limit
+        start = int(rng.integers(2, 100))
+        gaps = rng.integers(0, 4, len(prog))
+        pos = start
+        for ch, g in zip(prog, gaps):
+            if pos >= 128:
+                break
+            tape[pos] = enc[ch] if ch in enc else noop
+            pos += 1 + int(g) * (trial % 2)
+        if lang in ("bff", "bff_perm", "bff8", "bff_selfmove"):
+            tape[0] = rng.integers(0, 256)
+            tape[1] = rng.integers(0, 256)
+        check(host_lib, lang, tape)
+
+
 @pytest.mark.parametrize("lang", sorted(CRAFTED))
 def test_crafted_loops(host_lib, lang):
     for prog in CRAFTED[lang]:
