@@ -382,9 +382,6 @@ struct BffMachine {
   // h1 (they are not a fixed-destination sweep): enter_replay does not flag
   // them there.
   static constexpr uint32_t kCopySweep = 1u << 26;
-  // A body that moves no head: every iteration applies the same '+' / '-'
-  // and copies to the two bytes under the heads (reg_loop).
-  static constexpr uint32_t kStillLoop = 1u << 27;
   static constexpr int kReplayBatch = 8;  // replayed iterations per step call
 
   // Ops that a run of may merge into one replay op: head moves, copies (a
@@ -536,85 +533,9 @@ struct BffMachine {
       sweep = false;
     }
     rcls = ops;
-    bool still = !counter && kLogic != kLogicSelfmove;  // (bff_selfmove's copies move h1)
-    for (int o2 = 0; o2 < n && still; o2++) still = ((ops >> (8 * o2)) & 15) < kDec0;
     rpk = static_cast<uint32_t>(s) | (static_cast<uint32_t>(e) << 8) |
           (static_cast<uint32_t>(m) << 16) | (counter ? kCountLoop : 0u) |
-          (fixed ? kFixedTest : 0u) | (sweep ? kCopySweep : 0u) | (still ? kStillLoop : 0u);
-  }
-
-  // The bytes under h0 and h1 after `iters` iterations of a kStillLoop body
-  // from (a, b) (one byte when the heads coincide).
-  __host__ __device__ __forceinline__ void still_iterate(uint32_t &a, uint32_t &b,
-                                                         uint32_t iters) const {
-    const bool same = h0 == h1;
-    for (uint32_t it = 0; it < iters; it++) {
-      for (uint64_t w = rcls; w; w >>= 8) {
-        const uint32_t c = w & 15;
-        const uint32_t r = static_cast<uint32_t>((w >> 4) & 15) + 1;
-        if (c == kPlus) a += r;
-        else if (c == kMinus) a -= r;
-        else if (c == kCopy01) b = a;
-        else a = b;  // kCopy10
-        a &= 0xFF;
-        if (same) b = a;
-      }
-    }
-  }
-
-  // A loop of kStillLoop whose heads lie outside its code: its iterations
-  // only change the bytes under h0 and h1, by the same ops each time.  The
-  // iterations are run on those two bytes in registers until the ']' reads
-  // a zero under h0 (or the step limit allows no further whole iteration),
-  // and the bytes are written once.  After its first iteration the pair of
-  // bytes moves along a line (each copy ties one byte to the other) by a
-  // fixed step, so it repeats with a period dividing 256: 257 iterations
-  // without a zero mean none ever comes, and whole periods are skipped.
-  // Returns 1 when the program ended, 0 otherwise.
-  __host__ __device__ __forceinline__ int still_loop(const LaneBytes t, const LaneBytes snapa,
-                                                     const LaneNp np,
-                                                     const uint8_t *__restrict__ optab, int s,
-                                                     int e, int m, uint32_t len) {
-    const uint32_t lim = (kStepLimit - i) / len;  // whole iterations left, >= 1
-    const uint32_t a0 = v0, b0 = v1;
-    uint32_t a = a0, b = b0, k = 0;
-    bool found = false;
-    while (k < lim && k < 257) {
-      still_iterate(a, b, 1);
-      k++;
-      if ((a & kNullMask) == 0) {
-        found = true;
-        break;
-      }
-    }
-    if (!found && k < lim) {
-      // Periodic from iteration 1 on: the state after lim iterations is the
-      // state after 1 + (lim - 1) mod 256.
-      a = a0;
-      b = b0;
-      still_iterate(a, b, 1 + (lim - 1) % 256);
-      k = lim;
-    }
-    used0 = true;
-    if (h0 != h1) {
-      for (uint64_t w = rcls; w; w >>= 8)
-        if ((w & 15) == kCopy01 || (w & 15) == kCopy10) used1 = true;
-    }
-    write_fast(t, snapa, np, optab, h0, a0, a);
-    if (h1 != h0) write_fast(t, snapa, np, optab, h1, b0, b);
-    v0 = a;
-    v1 = h1 == h0 ? a : b;
-    i += k * len;
-    nskip += k * (len - 1 - static_cast<uint32_t>(m));
-    if (found) {  // the k-th ']' falls through
-      rpk = 0;
-      pc = e + 1;
-      if (pc >= kPair || i >= kStepLimit) return 1;
-      nxt = np.get(pc);
-      return 0;
-    }
-    pc = s + 1;
-    return i >= kStepLimit ? 1 : 0;
+          (fixed ? kFixedTest : 0u) | (sweep ? kCopySweep : 0u);
   }
 
   // A loop of kFixedTest whose ']' was taken once takes it every time: it
@@ -857,8 +778,6 @@ struct BffMachine {
       const int r = copy_sweep(t, snapa, np, optab, s, e, m, len);
       if (r >= 0) return r == 1;
     }
-    if ((rpk & kStillLoop) && (h0 < s || h0 > e) && (h1 < s || h1 > e))
-      return still_loop(t, snapa, np, optab, s, e, m, len) == 1;
     // Up to kReplayBatch iterations.
     for (int it = 0; it < kReplayBatch; it++) {
       if (it > 0 && i + len > kStepLimit) {
