@@ -412,6 +412,7 @@ int cubff_soup_set_epoch(cubff_soup *soup, uint64_t epoch, uint64_t reset_index)
   soup->epoch = epoch;
   soup->reset_index = reset_index;
   soup->pending_reset = false;
+  soup->perm_count = 0;  // the next run computes its pairings afresh
   return CUBFF_OK;
 }
 

@@ -227,7 +227,8 @@ int cubff_soup_read(cubff_soup *soup, uint8_t *dst, uint64_t offset,
 /* Epoch counter (the next epoch to run) and reset index (the index the
  * next reset will use, i.e. the value RunSimulation holds at a callback and
  * saves in checkpoints), restored from a checkpoint header
- * (common_language.h:354-360). */
+ * (common_language.h:354-360).  Pairings the soup computed ahead are
+ * dropped: the next run computes them again from this epoch. */
 int cubff_soup_set_epoch(cubff_soup *soup, uint64_t epoch, uint64_t reset_index);
 int cubff_soup_get_epoch(const cubff_soup *soup, uint64_t *epoch,
                          uint64_t *reset_index);
