@@ -44,7 +44,8 @@ struct ForthMachine {
   // Brent-schedule snapshot taken at a backward jump.
   int s_pos, s_sp;
   uint32_t s_mods, s_i, s_nops, s_power, s_lam;
-  uint64_t s_stk;          // stack[0 .. s_sp) packed, byte j at bits 8j (s_sp <= 8)
+  uint32_t s_top;          // stack[s_sp - 1] | stack[s_sp - 2] << 8 (0 where absent)
+  uint64_t s_mem;          // stack[0 .. s_sp - 2) packed, byte j at bits 8j (s_sp <= 8)
 
   // Stack slots at or above sp hold bytes left by an earlier pair; they are
   // never read before a push overwrites them.
@@ -58,7 +59,8 @@ struct ForthMachine {
     s_mods = s_i = s_nops = 0;
     s_power = 1;
     s_lam = 0;
-    s_stk = 0;
+    s_top = 0;
+    s_mem = 0;
   }
 
   __host__ __device__ __forceinline__ void push(const LaneBytes stk, uint32_t v) {
@@ -72,20 +74,23 @@ struct ForthMachine {
     }
   }
 
-  __host__ __device__ __forceinline__ uint64_t pack_stack(const LaneBytes stk) const {
+  // stack[0 .. sp - 2), the entries below the registers, packed.
+  __host__ __device__ __forceinline__ uint64_t pack_mem(const LaneBytes stk) const {
     uint64_t w = 0;
     for (int j = 0; j < sp - 2; j++) w |= static_cast<uint64_t>(stk.get(j)) << (8 * j);
-    if (sp >= 2) w |= static_cast<uint64_t>(r1) << (8 * (sp - 2));
-    if (sp >= 1) w |= static_cast<uint64_t>(r0) << (8 * (sp - 1));
     return w;
   }
 
   // At a step boundary right after a backward jump: when the state equals
   // the snapshot's, execution since the snapshot is periodic and whole periods
   // are skipped (i += k * P, nops += k * the period's no-ops); the snapshot is
-  // renewed after 1, 2, 4, ... visits.
+  // renewed after 1, 2, 4, ... visits.  The two entries in registers are
+  // compared first: a loop's counter usually sits on top, so most visits end
+  // there without reading the stack in memory.
   __host__ __device__ __forceinline__ void visit(const LaneBytes stk) {
-    if (pos == s_pos && sp == s_sp && mods == s_mods && pack_stack(stk) == s_stk) {
+    const uint32_t top = (sp >= 1 ? r0 : 0u) | ((sp >= 2 ? r1 : 0u) << 8);
+    if (pos == s_pos && sp == s_sp && mods == s_mods && top == s_top &&
+        (sp <= 2 || pack_mem(stk) == s_mem)) {
       const uint32_t period = i - s_i;
       const uint32_t k = (kStepLimit - i) / period;
       i += k * period;
@@ -97,7 +102,8 @@ struct ForthMachine {
       s_mods = mods;
       s_i = i;
       s_nops = nops;
-      s_stk = sp <= 8 ? pack_stack(stk) : 0;
+      s_top = top;
+      s_mem = (sp > 2 && sp <= 8) ? pack_mem(stk) : 0;
       s_power <<= 1;
       s_lam = 0;
     }

@@ -216,6 +216,39 @@ def test_crafted_loops(host_lib, lang):
         check(host_lib, lang, tape2)
 
 
+@pytest.mark.parametrize("lang", [lang for lang in LANGUAGES if lang.startswith("forth")])
+def test_forth_stack_edges(host_lib, lang):
+    """Forth programs built to reach the stack's edges: pops from an empty or
+    one-entry stack, dup / swap / add at depths 0-3, loops that push until the
+    stack overflows or pop it empty again, and tape writes that meet the
+    reset byte 0x13 (forthtrivial_reset) in the second half."""
+    rng = np.random.default_rng(4000 + LANGUAGES.index(lang))
+    ops = np.array(list(range(0, 14)) + [0x40, 0x41, 0x42, 0x7F, 0x07], dtype=np.uint8)
+    for trial in range(2000):
+        tape = np.full(128, 0x20, dtype=np.uint8)  # no-ops
+        pos = 0
+        for _ in range(int(rng.integers(0, 4))):  # a few constants first
+            tape[pos] = 0x40 | int(rng.integers(0, 64))
+            pos += 1
+        body = ops[rng.integers(0, ops.size, int(rng.integers(1, 10)))]
+        tape[pos:pos + body.size] = body
+        pos += body.size
+        kind = trial % 4
+        if kind == 0:  # loop back over the body (pushes until overflow, or pops)
+            tape[pos] = 0xC0 | (body.size - 1 + int(rng.integers(0, 2)))
+        elif kind == 1:  # a forward jump over a few bytes into more ops
+            tape[pos] = 0x80 | int(rng.integers(0, 4))
+            tape[pos + 1:pos + 8] = ops[rng.integers(0, ops.size, 7)]
+        elif kind == 2:  # a loop whose body pushes one entry per pass
+            tape[pos] = 0x41
+            tape[pos + 1] = 0xC0 | (body.size + 1)
+        if rng.random() < 0.5:
+            tape[64:] = np.where(rng.random(64) < 0.3, 0x13, tape[64:]).astype(np.uint8)
+        if rng.random() < 0.3:
+            tape[100:] = rng.integers(0, 256, 28, dtype=np.uint8)
+        check(host_lib, lang, tape)
+
+
 @pytest.mark.parametrize("lang", ["bff_noheads", "bff", "forth"])
 def test_long_running_pairs_of_an_evolved_soup(host_lib, lang):
     """The pairs of epoch 256 of an evolved soup (2^13 programs, seed 1) that
