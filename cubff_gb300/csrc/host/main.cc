@@ -1,8 +1,8 @@
 // main.cc — command-line driver of the GB300 engine with the reference CLI's
 // flags (main.cc:177-214) and its log format (main.cc:337-343, :391-401):
 //
-//   cubff_gb300/cubff_main --lang bff_noheads --max_epochs 256 \
-//       --disable_output --log out.csv --seed 10248
+//   cubff_gb300/cubff_main --lang bff_noheads --max_epochs 256
+//       --disable_output --log out.csv --seed 10248   (one command line)
 //
 // The soup runs on the device through LanguageInterface::RunSimulation.  The
 // terminal UI prints a summary line per callback; PPM drawing is not provided.

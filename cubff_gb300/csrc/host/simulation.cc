@@ -113,9 +113,10 @@ class Simulation : public LanguageInterface {
     RunSingleParsedProgram(ParseProgram(lang_, program), stepcount, debug);
   }
 
-  // EvalParsedSelfrep (common_language.h:326-342).
+  // EvalParsedSelfrep (common_language.h:326-342).  The device evaluation
+  // prints no intermediate programs, so debug has no effect.
   size_t EvalParsedSelfrep(std::vector<uint8_t> &parsed, size_t epoch, size_t seed,
-                           bool debug) override {
+                           bool /*debug*/) override {
     uint8_t prog[kSingleTapeSize] = {};
     std::memcpy(prog, parsed.data(), std::min(parsed.size(), sizeof(prog)));
     const uint64_t key = splitmix64(splitmix64(seed) ^ splitmix64(epoch));
