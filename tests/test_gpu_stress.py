@@ -1,5 +1,5 @@
-"""Repeated runs of small soups of every BFF-family language under several
-launch shapes, each against the oracle.
+"""Repeated runs of small soups of every BFF- and Forth-family language (and
+subleq) under several launch shapes, each against the oracle.
 
 A pipelined run is a dataflow over many warps whose interleaving changes
 from run to run; results must not.  Builds of the pipelined kernel whose code
@@ -22,7 +22,7 @@ SHAPES = [None,
           dict(lanes_per_pair64=48, steps_per_visit=128, claim_min=26, long_visits=2,
                first_visit_steps=8)]
 LANGS = ["bff", "bff_noheads", "bff_noheads_4bit", "bff_perm", "bff8", "bff8_noheads",
-         "bff_selfmove", "forth", "subleq"]
+         "bff_selfmove", "forth", "forthcopy", "forthtrivial", "forthtrivial_reset", "subleq"]
 N, SEED, EPOCHS, REPEATS = 1024, 41, 24, 6
 
 
