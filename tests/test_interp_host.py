@@ -130,7 +130,26 @@ CRAFTED = {
             b"\x05\x07+[}" + b"q" * 40 + b"]", b"\x05\x07+[}]" + b"+" * 10],
     "bff8": [b"\x05\x07+" + b"a" * 5 + b"]", b"\x05\x07" + b"]" * 8],
     "forth": [bytes([0x41, 0x04, 0x05, 0xC3]), bytes([0x20, 0xC1]), bytes([0x41, 0xC0]),
-              bytes([0x40, 0x07, 0xC2])],
+              bytes([0x40, 0x07, 0xC2]),
+              # the top two entries repeat at every backward jump while the entry
+              # below them counts (drop drop inc 5 6): the cycle check must also
+              # compare the stack in memory; period 256 passes
+              bytes([0x40, 0x45, 0x46, 0x05, 0x05, 0x08, 0x45, 0x46, 0xC4]),
+              # the same two entries deeper down (stack of 5, two fixed entries below)
+              bytes([0x47, 0x48, 0x40, 0x45, 0x46, 0x05, 0x05, 0x08, 0x45, 0x46, 0xC4]),
+              # nothing changes but the counter on top (inc, jump back to it):
+              # period 256 passes, runs to the step limit
+              bytes([0x41, 0x42, 0x43, 0x08, 0xC0]),
+              # as the first two, but the loop leaves when the counted entry wraps
+              # to 0 (if0 skips the forward jump out while it is not 0), after 256
+              # passes: a cycle check blind to the stack below the top two would
+              # skip to the step limit after the second pass
+              bytes([0x40, 0x45, 0x46, 0x05, 0x05, 0x08, 0x07, 0xBF, 0x45, 0x46, 0xC6]) +
+              b"\x20" * 117,
+              bytes([0x47, 0x48, 0x40, 0x45, 0x46, 0x05, 0x05, 0x08, 0x07, 0xBF, 0x45, 0x46,
+                     0xC6]) + b"\x20" * 115,
+              # the counter on top leaves the loop when it wraps to 0
+              bytes([0x41, 0x42, 0x43, 0x08, 0x07, 0xBF, 0xC2]) + b"\x20" * 121],
     "subleq": [bytes([5, 6, 0, 0, 0, 0, 0]), bytes([1, 1, 0])],
     "rsubleq4": [bytes([0, 0, 0, 0]), bytes([4, 5, 6, 0xFC])],
 }
@@ -249,7 +268,8 @@ def test_forth_stack_edges(host_lib, lang):
         check(host_lib, lang, tape)
 
 
-@pytest.mark.parametrize("lang", ["bff_noheads", "bff", "forth"])
+@pytest.mark.parametrize("lang", ["bff_noheads", "bff", "forth", "forthcopy", "forthtrivial",
+                                  "forthtrivial_reset"])
 def test_long_running_pairs_of_an_evolved_soup(host_lib, lang):
     """The pairs of epoch 256 of an evolved soup (2^13 programs, seed 1) that
     run longest: sweeping loops and counters that run to the step limit,
